@@ -1,0 +1,257 @@
+/*
+ * slaph_gb300.h — C ABI of the GB300 engine for the sLapH contraction hot path.
+ *
+ * The reference (pittlerf/sLapH-contractions) has no plugin or FFI layer: its
+ * hot path sits behind ordinary C++ classes that main/contract.cpp calls.  Each
+ * entry point below replaces one of those seams; the reference file:line it
+ * stands in for is given beside it.  Everything is plain C: opaque handles,
+ * plain pointers and sizes, int status codes (0 = ok), no exceptions across
+ * the boundary.  Complex numbers are interleaved (re, im) doubles, exactly the
+ * std::complex<double> byte layout the reference stores.
+ *
+ * Ownership: the caller owns every buffer it passes; the engine copies what it
+ * needs to device memory before a call returns.  The engine owns all device
+ * memory (eigenvectors, perambulators, noise, VdaggerV, factor caches).
+ *
+ * Threading: one host thread drives one engine.  Distinct engines are
+ * independent.
+ */
+#ifndef SLAPH_GB300_H
+#define SLAPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SLAPH_OK 0
+#define SLAPH_ERR_ARG 1         /* invalid argument or size mismatch            */
+#define SLAPH_ERR_CUDA 2        /* CUDA runtime error                           */
+#define SLAPH_ERR_STATE 3       /* call out of order (e.g. contract before VdV) */
+#define SLAPH_ERR_IO 4          /* file could not be opened / read / written    */
+#define SLAPH_ERR_EMPTY 5       /* empty random-vector combination; the
+                                   reference throws std::runtime_error here
+                                   (src/DilutedFactor.cpp:44-48,
+                                    src/DilutedTrace.cpp:37-41,131-135)          */
+#define SLAPH_ERR_UNSUPPORTED 6 /* feature not provided by this engine          */
+#define SLAPH_ERR_NOMEM 7       /* device or host allocation failed             */
+#define SLAPH_ERR_PARSE 8       /* infile could not be parsed                   */
+#define SLAPH_ERR_TIMEOUT 9     /* a bounded device wait gave up                */
+
+/* ---- enums ------------------------------------------------------------- */
+enum slaph_precision {
+  SLAPH_FP64 = 0,  /* every product in FP64                                   */
+  SLAPH_MIXED = 1  /* VdaggerV as split-BF16 tensor-core products with exact
+                      FP32 partial sums promoted to FP64; rest FP64            */
+};
+
+enum slaph_accumulator {
+  SLAPH_ACC_NATIVE = 0, /* NativeAccumulator (include/KahanAccumulator.hpp:50-72) */
+  SLAPH_ACC_KAHAN = 1   /* KahanAccumulator  (include/KahanAccumulator.hpp:14-48) */
+};
+
+/* Trace kinds, one per DilutedTrace*Factory of include/Diagram.hpp:44-89. */
+enum slaph_trace_kind {
+  SLAPH_TR_Q1 = 0,          /* "trQ1"            arity 1 */
+  SLAPH_TR_Q1Q1 = 1,        /* "trQ1Q1"          arity 2 */
+  SLAPH_TR_Q0Q2 = 2,        /* "trQ0Q2"          arity 2 */
+  SLAPH_TR_Q1Q1Q1 = 3,      /* "trQ1Q1Q1"        arity 3 */
+  SLAPH_TR_Q1Q0Q2 = 4,      /* "trQ1Q0Q2"        arity 3 */
+  SLAPH_TR_Q1Q1Q1Q1 = 5,    /* "trQ1Q1Q1Q1"      arity 4 */
+  SLAPH_TR_Q2Q0Q2Q0 = 6,    /* "trQ2Q0Q2Q0"      arity 4 */
+  SLAPH_TR_Q2Q0Q2Q0Q2Q0 = 7,/* "trQ2Q0Q2Q0Q2Q0"  arity 6 */
+  SLAPH_TR_KINDS = 8
+};
+
+#define SLAPH_MAX_DISP 8
+
+/* ---- plain-data mirrors of the reference lookup tables ----------------- */
+
+/* Lattice and dilution sizes shared by every call.  dilT is the number of
+ * time slices per dilution block, as contract() uses it
+ * (src/Correlators.cpp:65; DilutionScheme(Lt, dilT) in
+ *  include/dilution-iterator.hpp:312-313).  n_rnd is the total number of
+ * random vectors over all quark flavours (src/global_data.cpp:271-273). */
+typedef struct {
+  int32_t Lt, Lx, Ly, Lz;
+  int32_t nev;
+  int32_t dilT, dilE;
+  int32_t n_rnd;
+} slaph_dims;
+
+/* VdaggerVQuantumNumbers (include/typedefs.hpp:44-55).  disp holds n_disp
+ * (direction, axis) character pairs such as ('>', 'x'). */
+typedef struct {
+  int32_t id;
+  int32_t momentum[3];
+  int32_t n_disp;
+  char disp[2 * SLAPH_MAX_DISP];
+} slaph_vdv_op;
+
+/* DilutedFactorIndex (include/typedefs.hpp:105-121).  Only gamma[0] is used
+ * by the factor builders (src/DilutedFactorFactory.cpp:44,132,228). */
+typedef struct {
+  int32_t id_vdaggerv;
+  int32_t need_vdaggerv_daggering;
+  int32_t gamma;
+  int32_t n_rnd_pairs;
+  const int32_t *rnd_pairs; /* [n_rnd_pairs][2]: (first, second) */
+} slaph_factor_index;
+
+/* TraceRequest (include/global_data.hpp:72-81).  loc[i] is 0 for
+ * Location::source and 1 for Location::sink. */
+typedef struct {
+  int32_t kind; /* enum slaph_trace_kind */
+  int32_t tr_id;
+  int32_t n_loc;
+  int32_t loc[6];
+} slaph_trace_request;
+
+/* CorrelatorRequest (include/global_data.hpp:83-90). */
+typedef struct {
+  int32_t n_traces; /* 1, 2 or 3 */
+  slaph_trace_request traces[3];
+  const char *dataset_name;
+} slaph_correlator_request;
+
+/* One entry of CorrelatorRequestsMap (include/global_data.hpp:92). */
+typedef struct {
+  const char *name; /* "C2c", "C4cD", ... */
+  int32_t n_requests;
+  const slaph_correlator_request *requests;
+} slaph_diagram;
+
+/* All lookup tables that contract() receives (include/Correlators.hpp:41-54):
+ * OperatorLookup, DilutedFactorIndicesCollection ("Q0","Q1","Q2"),
+ * TraceIndicesCollection and CorrelatorRequestsMap, flattened.
+ * trace_ql_ids[k] is [n_trace_ids[k]][arity(k)] row-major.  Diagrams appear in
+ * the std::map order of the reference (sorted by name). */
+typedef struct {
+  int32_t n_vdv_ops;
+  const slaph_vdv_op *vdv_ops;
+  int32_t index_of_unity; /* -1 if absent */
+  int32_t need_gaugefield;
+  int32_t n_factors[3];
+  const slaph_factor_index *factors[3];
+  int32_t n_trace_ids[SLAPH_TR_KINDS];
+  const int32_t *trace_ql_ids[SLAPH_TR_KINDS];
+  int32_t n_diagrams;
+  const slaph_diagram *diagrams;
+} slaph_plan;
+
+/* Arity (number of quark lines) of a trace kind. */
+int slaph_trace_kind_arity(int kind);
+/* Name ("trQ0Q2", ...) of a trace kind, or NULL. */
+const char *slaph_trace_kind_name(int kind);
+
+/* ---- error reporting --------------------------------------------------- */
+/* Message of the last failed call made on this thread (never NULL). */
+const char *slaph_last_error(void);
+
+/* ---- front end: infile -> lookup tables -------------------------------- */
+/* Replaces read_parameters() (src/global_data.cpp:61-390) together with
+ * input_handling() (src/global_data_input_handling.cpp:249-275) and
+ * init_lookup_tables() (src/init_lookup_tables.cpp:470-556).
+ * argv (may be NULL) holds command-line overrides in the reference's
+ * "--key value" form, e.g. {"--start_config", "1000"}. */
+typedef struct slaph_frontend slaph_frontend;
+
+int slaph_frontend_create(const char *infile_path, int argc, const char *const *argv,
+                          slaph_frontend **out);
+int slaph_frontend_destroy(slaph_frontend *fe);
+/* Lattice and dilution sizes (dilT, dilE of quark 0, as main/contract.cpp:147,
+ * 180-181 passes them). */
+int slaph_frontend_dims(const slaph_frontend *fe, slaph_dims *out);
+/* Flattened lookup tables; the pointer stays valid until destroy. */
+int slaph_frontend_plan(const slaph_frontend *fe, const slaph_plan **out);
+/* Integer settings: "start_config", "end_config", "delta_config",
+ * "single_time_slice_combination", "n_quarks", "nb_eigen_threads". */
+int slaph_frontend_get_int(const slaph_frontend *fe, const char *key, int64_t *out);
+/* String settings: "output_path", "path_eigenvectors", "name_eigenvectors",
+ * "handling_vdaggerv", "path_vdaggerv", "path_config". */
+int slaph_frontend_get_str(const slaph_frontend *fe, const char *key, char *buf, size_t len);
+/* File names for one gauge configuration (build_IO_names,
+ * src/global_data_build_IO_names.cpp:76-85).  which: 0 = eigenvector prefix
+ * (append "%03d" t), 1 = perambulator of random vector index, 2 = random
+ * vector of index, 3 = correlator file suffix ("_cnfg%04d.h5"). */
+int slaph_frontend_io_name(const slaph_frontend *fe, int config, int which, int index,
+                           char *buf, size_t len);
+
+/* ---- input staging: the reference binary formats ------------------------ */
+/* EigenVector::read_eigen_vector (src/EigenVector.cpp:35-76): one timeslice,
+ * nev columns of 3*L^3 complex, column-major.  out: 2*3*L^3*nev doubles. */
+int slaph_read_eigenvectors(const char *path, int64_t dim_row, int32_t nev, double *out);
+/* Perambulator::read_perambulator (src/Perambulator.cpp:12-71) including the
+ * re-sort into (4*nev*Lt) x (Lt/dilT*dilE*dilD) column-major. */
+int slaph_read_perambulator(const char *path, int32_t Lt, int32_t nev, int32_t dilT,
+                            int32_t dilE, int32_t dilD, double *out);
+/* RandomVector::read_random_vector (src/RandomVector.cpp:87-113): Lt*4*nev
+ * complex entries, index dirac + 4*(ev + nev*t). */
+int slaph_read_random_vector(const char *path, int64_t length, double *out);
+
+/* ---- output: the reference HDF5 layout --------------------------------- */
+/* WriteHDF5Correlator (include/h5-wrapper.hpp:106-200,
+ * src/h5-wrapper.cpp:18-26): one file per diagram; one 1-D dataset of Lt
+ * compound {re f64, im f64} per correlator request.  data is
+ * [n_datasets][Lt][2].  Existing files are replaced. */
+int slaph_write_correlators_h5(const char *file_path, int32_t n_datasets,
+                               const char *const *dataset_names, int32_t Lt,
+                               const double *data);
+
+/* ---- engine ------------------------------------------------------------ */
+typedef struct slaph_engine slaph_engine;
+
+/* Creates an engine on the current CUDA device.  Allocates the device arrays
+ * for eigenvectors (all timeslices), perambulators and noise. */
+int slaph_engine_create(const slaph_dims *dims, slaph_engine **out);
+int slaph_engine_destroy(slaph_engine *eng);
+
+/* OperatorFactory ctor (src/OperatorFactory.cpp:184-218): the VdaggerV lookup
+ * table and the identity index.  Momentum phases are built on the device
+ * (create_momenta, src/OperatorFactory.cpp:64-95). */
+int slaph_engine_set_operators(slaph_engine *eng, const slaph_vdv_op *ops, int32_t n_ops,
+                               int32_t index_of_unity);
+/* Host -> device copies of the inputs (layouts as the readers above). */
+int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V);
+int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram);
+int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise);
+
+/* OperatorFactory::build_vdaggerv (src/OperatorFactory.cpp:220-326):
+ * VdaggerV[op][t] = V_t^dagger diag(exp(-ipx)) V_t for every op of the lookup,
+ * identity for index_of_unity.  precision: enum slaph_precision. */
+int slaph_vdaggerv_build(slaph_engine *eng, int precision);
+/* OperatorFactory::return_vdaggerv (include/OperatorsForMesons.hpp:66-69):
+ * nev x nev column-major complex into out (2*nev*nev doubles). */
+int slaph_vdaggerv_fetch(slaph_engine *eng, int32_t op_id, int32_t t, double *out);
+
+/* contract() (src/Correlators.cpp:40-127, include/Correlators.hpp:41-54).
+ * corr_out receives, for every diagram of plan (plan order) and every request
+ * (request order), Lt complex values C[t] = sum / Lt exactly as Diagram::write
+ * stores them (src/Diagram.cpp:132-147): [total_requests][Lt][2] doubles.
+ * single_block_pair >= 0 restricts the work to that block pair, as the
+ * reference's --single_time_slice_combination (src/Correlators.cpp:88-90). */
+int slaph_contract(slaph_engine *eng, const slaph_plan *plan, int precision, int accumulator,
+                   int single_block_pair, double *corr_out);
+/* Number of doubles slaph_contract writes for this plan. */
+int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt);
+
+/* Per-stage device times of the last build / contract, in milliseconds,
+ * measured with CUDA events on the engine stream.  out[0] VdaggerV,
+ * out[1] factors Q0/Q1/Q2, out[2] products + traces, out[3] assembly,
+ * out[4] host planning (wall clock), out[5] kernel launches issued.
+ * Returns the number of values written (<= n). */
+int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
+
+/* Device-resident statistics of the last contract: out[0] factors built,
+ * out[1] products, out[2] traces, out[3] correlator terms, out[4] flops of
+ * the factor stage, out[5] flops of products+traces. */
+int slaph_engine_stats(const slaph_engine *eng, double *out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLAPH_GB300_H */

@@ -1,0 +1,1068 @@
+// FP64 CPU oracle for the sLapH contraction hot path — TEST INFRASTRUCTURE.
+//
+// A restatement of the reference algorithm in plain C++17 + OpenMP, written to
+// follow the reference's own control flow (memoised factor and trace maps per
+// OpenMP thread, cleared per block pair) so that it reproduces the reference
+// outputs.  Each function names the reference file:line it follows.  Only the
+// tests, the smoke check and the CPU-baseline leg of bench.py use it.
+#include "oracle.h"
+
+#include <omp.h>
+
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+int g_threads = 0;
+
+using cd = std::complex<double>;
+
+inline cd mul(cd a, cd b) {
+  return {a.real() * b.real() - a.imag() * b.imag(),
+          a.real() * b.imag() + a.imag() * b.real()};
+}
+
+// Column-major complex matrix (the Eigen::MatrixXcd layout).
+struct Mat {
+  int r = 0, c = 0;
+  std::vector<cd> d;
+  Mat() = default;
+  Mat(int r_, int c_) : r(r_), c(c_), d(static_cast<size_t>(r_) * c_) {}
+  cd &operator()(int i, int j) { return d[i + static_cast<size_t>(r) * j]; }
+  cd operator()(int i, int j) const { return d[i + static_cast<size_t>(r) * j]; }
+  static Mat identity(int n) {
+    Mat m(n, n);
+    for (int i = 0; i < n; ++i) m(i, i) = 1.0;
+    return m;
+  }
+  Mat adjoint() const {
+    Mat m(c, r);
+    for (int j = 0; j < c; ++j)
+      for (int i = 0; i < r; ++i) m(j, i) = std::conj((*this)(i, j));
+    return m;
+  }
+};
+
+// C = A * B.
+Mat matmul(Mat const &A, Mat const &B) {
+  Mat C(A.r, B.c);
+  for (int j = 0; j < B.c; ++j)
+    for (int k = 0; k < A.c; ++k) {
+      cd const b = B(k, j);
+      cd const *a = &A.d[static_cast<size_t>(A.r) * k];
+      cd *cc = &C.d[static_cast<size_t>(C.r) * j];
+      for (int i = 0; i < A.r; ++i) cc[i] += mul(a[i], b);
+    }
+  return C;
+}
+
+// tr(L * R) = sum_i sum_k L(i,k) R(k,i).
+cd trace_of_product(Mat const &L, Mat const &R) {
+  cd s = 0;
+  for (int i = 0; i < L.r; ++i) {
+    cd row = 0;
+    for (int k = 0; k < L.c; ++k) row += mul(L(i, k), R(k, i));
+    s += row;
+  }
+  return s;
+}
+
+cd trace(Mat const &F) {
+  cd s = 0;
+  for (int i = 0; i < F.r; ++i) s += F(i, i);
+  return s;
+}
+
+// Neumaier / native accumulators, include/KahanAccumulator.hpp:14-72.
+struct Acc {
+  bool kahan = false;
+  cd sum = 0, c = 0;
+  explicit Acc(bool k) : kahan(k) {}
+  void add(cd x) {
+    if (!kahan) {
+      sum += x;
+      return;
+    }
+    cd const t = sum + x;
+    if (std::abs(sum) >= std::abs(x))
+      c += (sum - t) + x;
+    else
+      c += (x - t) + sum;
+    sum = t;
+  }
+  cd value() const { return kahan ? sum + c : sum; }
+};
+
+// ---------------------------------------------------------------- gamma
+// Dense tmLQCD basis (tests/gtest/gamma.cpp:22-40); the sparse table of
+// src/Gamma.cpp:18-246 is derived from it by products.
+struct GammaSparse {
+  int row[4];
+  cd value[4];
+};
+
+std::vector<GammaSparse> make_gamma_table() {
+  cd const I(0, 1);
+  using D = std::array<std::array<cd, 4>, 4>;
+  D g[4] = {};
+  g[0] = {{{0, 0, 1, 0}, {0, 0, 0, 1}, {1, 0, 0, 0}, {0, 1, 0, 0}}};
+  g[1] = {{{0, 0, 0, I}, {0, 0, I, 0}, {0, -I, 0, 0}, {-I, 0, 0, 0}}};
+  g[2] = {{{0, 0, 0, 1}, {0, 0, -1, 0}, {0, -1, 0, 0}, {1, 0, 0, 0}}};
+  g[3] = {{{0, 0, I, 0}, {0, 0, 0, -I}, {-I, 0, 0, 0}, {0, I, 0, 0}}};
+  auto prod = [](D const &a, D const &b) {
+    D c{};
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 4; ++k) c[i][j] += a[i][k] * b[k][j];
+    return c;
+  };
+  D one{};
+  for (int i = 0; i < 4; ++i) one[i][i] = 1;
+  D g5 = prod(prod(prod(g[0], g[1]), g[2]), g[3]);
+  std::vector<D> dense = {g[0],
+                          g[1],
+                          g[2],
+                          g[3],
+                          one,
+                          g5,
+                          prod(g[0], g5),
+                          prod(g[1], g5),
+                          prod(g[2], g5),
+                          prod(g[3], g5),
+                          prod(g[0], g[1]),
+                          prod(g[0], g[2]),
+                          prod(g[0], g[3]),
+                          prod(prod(g[0], g[1]), g5),
+                          prod(prod(g[0], g[2]), g5),
+                          prod(prod(g[0], g[3]), g5)};
+  std::vector<GammaSparse> out(16);
+  for (int m = 0; m < 16; ++m)
+    for (int col = 0; col < 4; ++col) {
+      int nz = -1;
+      for (int row = 0; row < 4; ++row)
+        if (std::abs(dense[m][row][col]) > 0.5) nz = row;
+      out[m].row[col] = nz;
+      out[m].value[col] = dense[m][nz][col];
+    }
+  return out;
+}
+
+std::vector<GammaSparse> const &gamma_table() {
+  static std::vector<GammaSparse> const t = make_gamma_table();
+  return t;
+}
+
+// ---------------------------------------------------------------- momenta
+// create_momenta, src/OperatorFactory.cpp:64-95.
+void create_momentum(int Lx, int Ly, int Lz, const int p[3], cd *out) {
+  static const cd I(0.0, 1.0);
+  double const ipx = p[0] * 2. * M_PI / static_cast<double>(Lx);
+  double const ipy = p[1] * 2. * M_PI / static_cast<double>(Ly);
+  double const ipz = p[2] * 2. * M_PI / static_cast<double>(Lz);
+  for (int x = 0; x < Lx; ++x) {
+    int const xH = x * Ly * Lz;
+    double const ipxH = ipx * x;
+    for (int y = 0; y < Ly; ++y) {
+      int const xHyH = xH + y * Lz;
+      double const ipxHipyH = ipxH + ipy * y;
+      for (int z = 0; z < Lz; ++z) out[xHyH + z] = std::exp(-I * (ipxHipyH + ipz * z));
+    }
+  }
+}
+
+// C (n x n) = A^H B for A, B of K x n (column-major), blocked over K.
+void gemm_ah_b(cd const *A, cd const *B, long K, int n, cd *C) {
+  for (long i = 0; i < static_cast<long>(n) * n; ++i) C[i] = 0;
+  long const KB = 96;
+  for (long k0 = 0; k0 < K; k0 += KB) {
+    long const kb = std::min(KB, K - k0);
+    for (int j = 0; j < n; j += 2) {
+      int const nj = std::min(2, n - j);
+      for (int i = 0; i < n; i += 2) {
+        int const ni = std::min(2, n - i);
+        double acc[2][2][2] = {};
+        for (int jj = 0; jj < nj; ++jj)
+          for (int ii = 0; ii < ni; ++ii) {
+            double const *a = reinterpret_cast<double const *>(A + K * (i + ii) + k0);
+            double const *b = reinterpret_cast<double const *>(B + K * (j + jj) + k0);
+            double sr = 0, si = 0;
+            for (long k = 0; k < kb; ++k) {
+              double const ar = a[2 * k], ai = a[2 * k + 1];
+              double const br = b[2 * k], bi = b[2 * k + 1];
+              sr += ar * br + ai * bi;
+              si += ar * bi - ai * br;
+            }
+            acc[ii][jj][0] = sr;
+            acc[ii][jj][1] = si;
+          }
+        for (int jj = 0; jj < nj; ++jj)
+          for (int ii = 0; ii < ni; ++ii)
+            C[(i + ii) + static_cast<long>(n) * (j + jj)] +=
+                cd(acc[ii][jj][0], acc[ii][jj][1]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- dilution
+enum class DilType { block, interlace };
+
+// BlockIterator, include/dilution-iterator.hpp:21-191.
+struct BlockIter {
+  int slice_source, slice_sink, block_source, block_sink, num_slice, num_block, pass;
+  DilType type;
+  void next() {
+    int const bs = num_slice / num_block;
+    if (type == DilType::block) {
+      int const src_begin = block_source * bs, src_end = (block_source + 1) * bs;
+      int const snk_begin = block_sink * bs, snk_end = (block_sink + 1) * bs;
+      ++slice_sink;
+      if (slice_sink == snk_end) {
+        slice_sink = snk_begin;
+        ++slice_source;
+      }
+      if (slice_source == src_end) {
+        slice_source = snk_begin;
+        slice_sink = src_begin;
+        ++pass;
+        if (block_source == block_sink) ++pass;
+        std::swap(block_source, block_sink);
+      }
+    } else {
+      int const src_begin = block_source, snk_begin = block_sink;
+      slice_sink += bs;
+      if (slice_sink >= num_slice) {
+        slice_sink = snk_begin;
+        slice_source += bs;
+      }
+      if (slice_source >= num_slice) {
+        slice_source = snk_begin;
+        slice_sink = src_begin;
+        ++pass;
+        if (block_source == block_sink) ++pass;
+        std::swap(block_source, block_sink);
+      }
+    }
+  }
+};
+
+// DilutionScheme, include/dilution-iterator.hpp:306-356 (block size = dilT).
+struct DilScheme {
+  int num_slice, num_block;
+  DilType type;
+  DilScheme(int ns, int block_size, DilType t)
+      : num_slice(ns), num_block(ns / block_size), type(t) {}
+  int size() const { return num_block * (num_block + 1) / 2; }
+  std::pair<int, int> blocks(int i) const {
+    int bsnk = 0, bsrc = 0;
+    for (int j = 0; j < i; ++j) {
+      ++bsnk;
+      if (bsnk == num_block) {
+        ++bsrc;
+        bsnk = bsrc;
+      }
+    }
+    return {bsrc, bsnk};
+  }
+  std::vector<std::pair<int, int>> slices(int i) const {
+    auto b = blocks(i);
+    int const bs = num_slice / num_block;
+    BlockIter it{};
+    if (type == DilType::block)
+      it = {b.first * bs, b.second * bs, b.first, b.second, num_slice, num_block, 0, type};
+    else
+      it = {b.first, b.second, b.first, b.second, num_slice, num_block, 0, type};
+    std::vector<std::pair<int, int>> out;
+    // end(): same blocks/sizes, pass 2; comparison ignores slices
+    // (include/dilution-iterator.hpp:126-130).
+    int const b0 = b.first, b1 = b.second;
+    while (!((it.block_source == b0 && it.block_sink == b1 && it.pass == 2))) {
+      out.emplace_back(it.slice_source, it.slice_sink);
+      it.next();
+      if (out.size() > static_cast<size_t>(4 * num_slice * num_slice))
+        throw std::runtime_error("dilution iterator did not terminate");
+    }
+    return out;
+  }
+  int time_to_block(int t) const {
+    int const bs = num_slice / num_block;
+    return type == DilType::block ? t / bs : t % bs;
+  }
+};
+
+// ---------------------------------------------------------------- factors
+struct DF {  // DilutedFactor, include/DilutedFactor.hpp:19-25
+  Mat data;
+  int r1, r2;
+  uint16_t used;
+};
+using DFList = std::vector<DF>;
+using DFMap = std::map<long, DFList>;  // operator key -> factors
+
+struct DT {  // DilutedTrace, include/DilutedTrace.hpp:7-12
+  cd data;
+  uint16_t used;
+};
+using DTMap = std::map<long, std::vector<DT>>;
+
+struct Inputs {
+  slaph_dims dims;
+  slaph_plan const *plan;
+  double const *vdv;            // [n_ops][Lt][nev][nev]
+  double const *const *peram;   // [n_rnd]
+  double const *noise;          // [n_rnd][Lt*4*nev]
+  int n_ops;
+  bool kahan;
+
+  long peram_rows() const { return 4L * dims.nev * dims.Lt; }
+  cd P(int r, long row, long col) const {
+    double const *p = peram[r] + 2 * (row + peram_rows() * col);
+    return {p[0], p[1]};
+  }
+  cd rnd(int r, long blk) const {
+    double const *p = noise + 2 * (static_cast<long>(r) * dims.Lt * 4 * dims.nev + blk);
+    return {p[0], p[1]};
+  }
+  // return_vdaggerv + optional adjoint (src/DilutedFactorFactory.cpp:49-58).
+  Mat vdaggerv(slaph_factor_index const &op, int t) const {
+    int const n = dims.nev;
+    if (op.id_vdaggerv < 0 || op.id_vdaggerv >= n_ops)
+      throw std::runtime_error("VdaggerV id out of range");
+    Mat m(n, n);
+    double const *src =
+        vdv + 2 * (static_cast<long>(op.id_vdaggerv) * dims.Lt + t) * n * static_cast<long>(n);
+    std::memcpy(static_cast<void *>(m.d.data()), src, sizeof(cd) * n * static_cast<size_t>(n));
+    return op.need_vdaggerv_daggering ? m.adjoint() : m;
+  }
+  // peram[r].block(row0, col0, nr, nc)
+  Mat peram_block(int r, long row0, long col0, int nr, int nc) const {
+    Mat m(nr, nc);
+    for (int j = 0; j < nc; ++j)
+      for (int i = 0; i < nr; ++i) m(i, j) = P(r, row0 + i, col0 + j);
+    return m;
+  }
+};
+
+constexpr int dilD = 4;
+
+// DilutedFactorFactory<Q0>::build, src/DilutedFactorFactory.cpp:34-101.
+void build_q0(Inputs const &in, int t1, std::map<std::array<int, 1>, DFMap> &Ql) {
+  int const nev = in.dims.nev, dilE = in.dims.dilE, eds = dilD * dilE;
+  auto const &gam = gamma_table();
+  auto &dst = Ql[{t1}];
+  for (int opk = 0; opk < in.plan->n_factors[0]; ++opk) {
+    auto const &op = in.plan->factors[0][opk];
+    Mat const vdv = in.vdaggerv(op, t1);
+    int check = -1;
+    Mat M;
+    for (int k = 0; k < op.n_rnd_pairs; ++k) {
+      int const r1 = op.rnd_pairs[2 * k], r2 = op.rnd_pairs[2 * k + 1];
+      if (check != r2) {
+        M = Mat(nev, 4 * dilE);
+        for (int v = 0; v < nev; ++v)
+          for (int block = 0; block < 4; ++block) {
+            long const blk = block + (v + static_cast<long>(nev) * t1) * 4;
+            cd const rr = in.rnd(r2, blk);
+            int const col = v % dilE + dilE * block;
+            for (int i = 0; i < nev; ++i) M(i, col) += mul(rr, vdv(i, v));
+          }
+      }
+      Mat matrix(eds, eds);
+      for (int block = 0; block < 4; ++block) {
+        cd const value = gam[op.gamma].value[block];
+        int const gi = gam[op.gamma].row[block];
+        for (int v = 0; v < nev; ++v) {
+          long const blk = gi + (v + static_cast<long>(nev) * t1) * dilD;
+          cd const cr = std::conj(in.rnd(r1, blk));
+          for (int e = 0; e < dilE; ++e)
+            matrix(v % dilE + dilE * gi, block * dilE + e) +=
+                mul(mul(value, M(v, block * dilE + e)), cr);
+        }
+      }
+      check = r2;
+      dst[opk].push_back({std::move(matrix), r1, r2, 0});
+    }
+  }
+}
+
+// DilutedFactorFactory<Q1>::build, src/DilutedFactorFactory.cpp:104-170.
+void build_q1(Inputs const &in, int t1, int b2, std::map<std::array<int, 2>, DFMap> &Ql) {
+  int const nev = in.dims.nev, dilE = in.dims.dilE, eds = dilD * dilE;
+  auto const &gam = gamma_table();
+  auto &dst = Ql[{t1, b2}];
+  for (int opk = 0; opk < in.plan->n_factors[1]; ++opk) {
+    auto const &op = in.plan->factors[1][opk];
+    Mat const vdv = in.vdaggerv(op, t1);
+    for (int k = 0; k < op.n_rnd_pairs; ++k) {
+      int const r1 = op.rnd_pairs[2 * k], r2 = op.rnd_pairs[2 * k + 1];
+      Mat rvdv(eds, nev);
+      for (int v = 0; v < nev; ++v)
+        for (int block = 0; block < dilD; ++block) {
+          long const blk = block + v * dilD + static_cast<long>(dilD) * nev * t1;
+          cd const cr = std::conj(in.rnd(r1, blk));
+          int const row = v % dilE + dilE * block;
+          for (int j = 0; j < nev; ++j) rvdv(row, j) += mul(cr, vdv(v, j));
+        }
+      Mat matrix(eds, eds);
+      for (int row = 0; row < dilD; ++row) {
+        cd const value = gam[op.gamma].value[row];
+        Mat A(dilE, nev);
+        for (int j = 0; j < nev; ++j)
+          for (int i = 0; i < dilE; ++i) A(i, j) = rvdv(row * dilE + i, j);
+        for (int col = 0; col < dilD; ++col) {
+          Mat const B = in.peram_block(r2, (static_cast<long>(t1) * dilD + gam[op.gamma].row[row]) * nev,
+                                       (static_cast<long>(b2) * dilD + col) * dilE, nev, dilE);
+          Mat const AB = matmul(A, B);
+          for (int j = 0; j < dilE; ++j)
+            for (int i = 0; i < dilE; ++i)
+              matrix(row * dilE + i, col * dilE + j) = mul(value, AB(i, j));
+        }
+      }
+      dst[opk].push_back({std::move(matrix), r1, r2, 0});
+    }
+  }
+}
+
+// DilutedFactorFactory<Q2>::build, src/DilutedFactorFactory.cpp:173-253.
+void build_q2(Inputs const &in, int b1, int t1, int b2,
+              std::map<std::array<int, 3>, DFMap> &Ql) {
+  int const nev = in.dims.nev, dilE = in.dims.dilE, eds = dilD * dilE;
+  auto const &gam = gamma_table();
+  auto &dst = Ql[{b1, t1, b2}];
+  for (int opk = 0; opk < in.plan->n_factors[2]; ++opk) {
+    auto const &op = in.plan->factors[2][opk];
+    Mat const vdv = in.vdaggerv(op, t1);
+    Mat M(dilD * dilE, 4 * nev);
+    int check = -1;
+    for (int k = 0; k < op.n_rnd_pairs; ++k) {
+      int const r1 = op.rnd_pairs[2 * k], r2 = op.rnd_pairs[2 * k + 1];
+      if (check != r1) {
+        for (int row = 0; row < dilD; ++row)
+          for (int col = 0; col < 4; ++col) {
+            Mat const Pb = in.peram_block(r1, (static_cast<long>(t1) * 4 + row) * nev,
+                                          (static_cast<long>(b1) * dilD + col) * dilE, nev,
+                                          dilE);
+            Mat const blk = matmul(Pb.adjoint(), vdv);
+            bool const flip = ((row + col) == 3) || (std::abs(row - col) > 1);
+            for (int j = 0; j < nev; ++j)
+              for (int i = 0; i < dilE; ++i)
+                M(col * dilE + i, row * nev + j) = flip ? -blk(i, j) : blk(i, j);
+          }
+      }
+      Mat matrix(eds, eds);
+      for (int bd = 0; bd < dilD; ++bd) {
+        cd const value = gam[op.gamma].value[bd];
+        int const gi = gam[op.gamma].row[bd];
+        for (int row = 0; row < dilD; ++row) {
+          Mat A(dilE, nev);
+          for (int j = 0; j < nev; ++j)
+            for (int i = 0; i < dilE; ++i) A(i, j) = mul(value, M(row * dilE + i, bd * nev + j));
+          for (int col = 0; col < dilD; ++col) {
+            Mat const B = in.peram_block(r2, (static_cast<long>(t1) * 4 + gi) * nev,
+                                         (static_cast<long>(b2) * dilD + col) * dilE, nev, dilE);
+            Mat const AB = matmul(A, B);
+            for (int j = 0; j < dilE; ++j)
+              for (int i = 0; i < dilE; ++i) matrix(row * dilE + i, col * dilE + j) += AB(i, j);
+          }
+        }
+      }
+      check = r1;
+      dst[opk].push_back({std::move(matrix), r1, r2, 0});
+    }
+  }
+}
+
+template <int N, typename BuildFn>
+struct FactorFactory {
+  std::map<std::array<int, N>, DFMap> Ql;
+  BuildFn fn;
+  explicit FactorFactory(BuildFn f) : fn(f) {}
+  DFMap const &operator[](std::array<int, N> const &key) {
+    if (Ql.count(key) == 0) fn(key, Ql);
+    return Ql.at(key);
+  }
+  void clear() { Ql.clear(); }
+};
+
+// operator*(vector<DF>, vector<DF>), src/DilutedFactor.cpp:6-51.
+DFList operator*(DFList const &L, DFList const &R) {
+  DFList out;
+  for (auto const &l : L) {
+    int const inner = l.r2;
+    for (auto const &r : R) {
+      if (!(inner == r.r1 && l.r1 != r.r2)) continue;
+      if ((l.used & r.used) != 0u) continue;
+      uint16_t const used = l.used | r.used | static_cast<uint16_t>(1u << inner);
+      out.push_back({matmul(l.data, r.data), l.r1, r.r2, used});
+    }
+  }
+  if (out.empty())
+    throw std::runtime_error(
+        "vector<DilutedFactor> operator*(vector<DilutedFactor>, vector<DilutedFactor>) "
+        "has an empty result.");
+  return out;
+}
+
+// factor_to_trace(L, R), src/DilutedTrace.cpp:84-138.
+std::vector<DT> factor_to_trace(DFList const &L, DFList const &R) {
+  std::vector<DT> out;
+  for (auto const &l : L) {
+    int const outer = l.r1, inner = l.r2;
+    for (auto const &r : R) {
+      if (!(inner == r.r1 && outer == r.r2)) continue;
+      if ((l.used & r.used) != 0u) continue;
+      uint16_t const used = l.used | r.used | static_cast<uint16_t>(1u << inner) |
+                            static_cast<uint16_t>(1u << outer);
+      out.push_back({trace_of_product(l.data, r.data), used});
+    }
+  }
+  if (out.empty())
+    throw std::runtime_error(
+        "vector<DilutedTrace> factor_to_trace(vector<DilutedFactor>, "
+        "vector<DilutedFactor>) has an empty result. Not enough random vectors?");
+  return out;
+}
+
+// factor_to_trace(vec), src/DilutedTrace.cpp:140-165.
+std::vector<DT> factor_to_trace(DFList const &v) {
+  std::vector<DT> out;
+  for (auto const &e : v) {
+    if (e.r1 != e.r2) continue;
+    out.push_back({trace(e.data), static_cast<uint16_t>(e.used | (1u << e.r1))});
+  }
+  if (out.empty())
+    throw std::runtime_error(
+        "vector<DilutedTrace> factor_to_trace(vector<DilutedFactor>) has an empty "
+        "result.");
+  return out;
+}
+
+// multiply<1,1>, include/DilutedFactor.hpp:164-187.
+void multiply(std::map<std::array<long, 2>, DFList> &L, std::array<long, 2> const &key,
+              DFMap const &f0, DFMap const &f1) {
+  if (L.count(key) == 0) L[key] = f0.at(key[0]) * f1.at(key[1]);
+}
+
+// ---------------------------------------------------------------- parts
+struct Parts {  // DiagramParts, include/Diagram.hpp:12-107
+  Inputs const &in;
+  DilScheme const &ds;
+  std::function<void(std::array<int, 1> const &, std::map<std::array<int, 1>, DFMap> &)> f0;
+  std::function<void(std::array<int, 2> const &, std::map<std::array<int, 2>, DFMap> &)> f1;
+  std::function<void(std::array<int, 3> const &, std::map<std::array<int, 3>, DFMap> &)> f2;
+  FactorFactory<1, decltype(f0)> q0;
+  FactorFactory<2, decltype(f1)> q1;
+  FactorFactory<3, decltype(f2)> q2;
+  std::map<std::vector<int>, DTMap> tr[SLAPH_TR_KINDS];
+
+  Parts(Inputs const &in_, DilScheme const &ds_)
+      : in(in_),
+        ds(ds_),
+        f0([this](std::array<int, 1> const &k, std::map<std::array<int, 1>, DFMap> &m) {
+          build_q0(in, k[0], m);
+        }),
+        f1([this](std::array<int, 2> const &k, std::map<std::array<int, 2>, DFMap> &m) {
+          build_q1(in, k[0], k[1], m);
+        }),
+        f2([this](std::array<int, 3> const &k, std::map<std::array<int, 3>, DFMap> &m) {
+          build_q2(in, k[0], k[1], k[2], m);
+        }),
+        q0(f0),
+        q1(f1),
+        q2(f2) {}
+
+  void clear() {
+    q0.clear();
+    q1.clear();
+    q2.clear();
+    // DilutedTrace1Factory::clear() keeps its cache
+    // (include/DilutedTraceFactory.hpp:61).
+    for (int k = 1; k < SLAPH_TR_KINDS; ++k) tr[k].clear();
+  }
+
+  int const *ids(int kind, long i) const {
+    static int const arity[SLAPH_TR_KINDS] = {1, 2, 2, 3, 3, 4, 4, 6};
+    return in.plan->trace_ql_ids[kind] + i * arity[kind];
+  }
+  long n_ids(int kind) const { return in.plan->n_trace_ids[kind]; }
+  int blk(int t) const { return ds.time_to_block(t); }
+
+  // DilutedTrace*Factory::build, src/DilutedTraceFactory.cpp:13-245.
+  void build(int kind, std::vector<int> const &t, DTMap &out) {
+    using K2 = std::array<long, 2>;
+    switch (kind) {
+      case SLAPH_TR_Q1: {
+        int const b = blk(t[0]);
+        for (long i = 0; i < n_ids(kind); ++i)
+          out[i] = factor_to_trace(q1[{t[0], b}].at(ids(kind, i)[0]));
+        break;
+      }
+      case SLAPH_TR_Q1Q1: {
+        int const b1 = blk(t[0]), b2 = blk(t[1]);
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          DFList const &l = q1[{t[0], b2}].at(c[0]);
+          DFList const &r = q1[{t[1], b1}].at(c[1]);
+          out[i] = factor_to_trace(l, r);
+        }
+        break;
+      }
+      case SLAPH_TR_Q0Q2: {
+        int const b2 = blk(t[1]);
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          DFList const &l = q0[{t[1]}].at(c[1]);
+          DFList const &r = q2[{b2, t[0], b2}].at(c[0]);
+          out[i] = factor_to_trace(l, r);
+        }
+        break;
+      }
+      case SLAPH_TR_Q1Q1Q1: {
+        int const b1 = blk(t[0]), b2 = blk(t[1]), b3 = blk(t[2]);
+        std::map<K2, DFList> L1;
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          DFMap const &a = q1[{t[0], b2}];
+          DFMap const &b = q1[{t[1], b3}];
+          multiply(L1, {c[0], c[1]}, a, b);
+        }
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          DFList const &r = q1[{t[2], b1}].at(c[2]);
+          out[i] = factor_to_trace(L1[{c[0], c[1]}], r);
+        }
+        break;
+      }
+      case SLAPH_TR_Q1Q0Q2: {
+        int const b1 = blk(t[0]), b2 = blk(t[1]), b3 = blk(t[2]);
+        std::map<K2, DFList> L1;
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          DFMap const &a = q0[{t[0]}];
+          DFMap const &b = q2[{b1, t[0], b2}];
+          multiply(L1, {c[2], c[0]}, a, b);
+        }
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          DFList const &r = q1[{t[1], b3}].at(c[1]);
+          out[i] = factor_to_trace(L1[{c[2], c[0]}], r);
+        }
+        break;
+      }
+      case SLAPH_TR_Q1Q1Q1Q1: {
+        int const b0 = blk(t[0]), b1 = blk(t[1]), b2 = blk(t[2]), b3 = blk(t[3]);
+        std::map<K2, DFList> L1, L2;
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          {
+            DFMap const &a = q1[{t[0], b1}];
+            DFMap const &b = q1[{t[1], b2}];
+            multiply(L1, {c[0], c[1]}, a, b);
+          }
+          {
+            DFMap const &a = q1[{t[2], b3}];
+            DFMap const &b = q1[{t[3], b0}];
+            multiply(L2, {c[2], c[3]}, a, b);
+          }
+        }
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          out[i] = factor_to_trace(L1[{c[0], c[1]}], L2[{c[2], c[3]}]);
+        }
+        break;
+      }
+      case SLAPH_TR_Q2Q0Q2Q0: {
+        int const b0 = blk(t[0]), b2 = blk(t[2]);
+        std::map<K2, DFList> L1, L2;
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          {
+            DFMap const &a = q0[{t[0]}];
+            DFMap const &b = q2[{b0, t[1], b2}];
+            multiply(L1, {c[0], c[1]}, a, b);
+          }
+          {
+            DFMap const &a = q0[{t[2]}];
+            DFMap const &b = q2[{b2, t[3], b0}];
+            multiply(L2, {c[2], c[3]}, a, b);
+          }
+        }
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          out[i] = factor_to_trace(L1[{c[0], c[1]}], L2[{c[2], c[3]}]);
+        }
+        break;
+      }
+      case SLAPH_TR_Q2Q0Q2Q0Q2Q0: {
+        int const b1 = blk(t[1]), b3 = blk(t[3]), b5 = blk(t[5]);
+        for (long i = 0; i < n_ids(kind); ++i) {
+          auto c = ids(kind, i);
+          DFMap const &m0 = q2[{b5, t[0], b1}];
+          DFMap const &m1 = q0[{t[1]}];
+          DFMap const &m2 = q2[{b1, t[2], b3}];
+          DFMap const &m3 = q0[{t[3]}];
+          DFMap const &m4 = q2[{b3, t[4], b5}];
+          DFMap const &m5 = q0[{t[5]}];
+          DFList const p = (((m0.at(c[1]) * m1.at(c[2])) * m2.at(c[3])) * m3.at(c[4])) *
+                           m4.at(c[5]);
+          out[i] = factor_to_trace(p, m5.at(c[0]));
+        }
+        break;
+      }
+      default:
+        throw std::runtime_error("unknown trace kind");
+    }
+  }
+
+  // AbstractDilutedTraceFactory::get, include/DilutedTraceFactory.hpp:52-57.
+  std::vector<DT> const &get(slaph_trace_request const &r, int src, int snk) {
+    std::vector<int> key(r.n_loc);
+    for (int l = 0; l < r.n_loc; ++l) key[l] = r.loc[l] == 0 ? src : snk;
+    auto &m = tr[r.kind];
+    auto it = m.find(key);
+    if (it == m.end()) {
+      DTMap built;
+      build(r.kind, key, built);
+      it = m.emplace(key, std::move(built)).first;
+    }
+    return it->second.at(r.tr_id);
+  }
+};
+
+// inner_product, src/DilutedTrace.cpp:5-82.
+cd inner_product(std::vector<DT> const &L, std::vector<DT> const &R, bool kahan) {
+  long num = 0;
+  Acc result(kahan);
+  for (auto const &l : L) {
+    Acc right_sum(kahan);
+    for (auto const &r : R) {
+      if ((l.used & r.used) != 0u) continue;
+      right_sum.add(r.data);
+      ++num;
+    }
+    result.add(l.data * right_sum.value());
+  }
+  if (num == 0)
+    throw std::runtime_error(
+        "compcomp_t inner_product(vector<DilutedTrace>, vector<DilutedTrace>) has an empty "
+        "result. Not enough random vectors?");
+  return result.value() / static_cast<double>(num);
+}
+
+cd inner_product(std::vector<DT> const &L, std::vector<DT> const &M, std::vector<DT> const &R,
+                 bool kahan) {
+  long num = 0;
+  Acc result(kahan);
+  for (auto const &l : L)
+    for (auto const &m : M) {
+      Acc right_sum(kahan);
+      for (auto const &r : R) {
+        if ((l.used & m.used & r.used) != 0u) continue;
+        right_sum.add(r.data);
+        ++num;
+      }
+      result.add(l.data * m.data * right_sum.value());
+    }
+  if (num == 0)
+    throw std::runtime_error(
+        "compcomp_t inner_product(vector<DilutedTrace>, vector<DilutedTrace>) has an empty "
+        "result. Not enough random vectors?");
+  return result.value() / static_cast<double>(num);
+}
+
+// resolve_request{1,2,3}, src/Diagram.cpp:9-94.
+cd resolve(slaph_correlator_request const &req, int src, int snk, Parts &q, bool kahan) {
+  if (req.n_traces == 1) {
+    auto const &x = q.get(req.traces[0], src, snk);
+    Acc a(kahan);
+    for (auto const &e : x) a.add(e.data);
+    return a.value() / static_cast<double>(x.size());
+  }
+  if (req.n_traces == 2) {
+    auto const &x0 = q.get(req.traces[0], src, snk);
+    auto const &x1 = q.get(req.traces[1], src, snk);
+    return inner_product(x0, x1, kahan);
+  }
+  if (req.n_traces == 3) {
+    auto const &x0 = q.get(req.traces[0], src, snk);
+    auto const &x1 = q.get(req.traces[1], src, snk);
+    auto const &x2 = q.get(req.traces[2], src, snk);
+    return inner_product(x0, x1, x2, kahan);
+  }
+  throw std::runtime_error("This many traces are not implemented yet.");
+}
+
+void check_dims(slaph_dims const *d) {
+  if (!d || d->Lt < 1 || d->Lx < 1 || d->Ly < 1 || d->Lz < 1 || d->nev < 1 || d->dilT < 1 ||
+      d->dilE < 1 || d->Lt % d->dilT != 0)
+    throw std::runtime_error("invalid dims");
+}
+
+template <typename F>
+int guarded(F &&f) {
+  try {
+    f();
+    return SLAPH_OK;
+  } catch (std::exception const &e) {
+    g_err = e.what();
+    return SLAPH_ERR_ARG;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *oracle_last_error(void) { return g_err.c_str(); }
+
+int oracle_threads(void) { return g_threads > 0 ? g_threads : omp_get_max_threads(); }
+void oracle_set_threads(int n) { g_threads = n; }
+
+void oracle_create_momentum(int Lx, int Ly, int Lz, const int p[3], double *out) {
+  create_momentum(Lx, Ly, Lz, p, reinterpret_cast<cd *>(out));
+}
+
+void oracle_gamma_table(int32_t *row, double *value) {
+  auto const &g = gamma_table();
+  for (int m = 0; m < 16; ++m)
+    for (int c = 0; c < 4; ++c) {
+      row[4 * m + c] = g[m].row[c];
+      value[2 * (4 * m + c)] = g[m].value[c].real();
+      value[2 * (4 * m + c) + 1] = g[m].value[c].imag();
+    }
+}
+
+int oracle_vdaggerv(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
+                    int index_of_unity, const double *const *V, const int *ts, int n_ts,
+                    double *out) {
+  return guarded([&] {
+    check_dims(dims);
+    int const nev = dims->nev;
+    long const vol = static_cast<long>(dims->Lx) * dims->Ly * dims->Lz;
+    long const dim_row = 3 * vol;
+    for (int i = 0; i < n_ops; ++i) {
+      if (ops[i].id != i) throw std::runtime_error("VdaggerV ids must be 0..n_ops-1");
+      if (ops[i].n_disp != 0 && ops[i].id != index_of_unity)
+        throw std::runtime_error("displaced operators need a gauge field");
+    }
+    // momentum[op.id][x], src/OperatorFactory.cpp:209-215.
+    std::vector<cd> momentum(static_cast<size_t>(n_ops) * vol);
+    for (int i = 0; i < n_ops; ++i)
+      create_momentum(dims->Lx, dims->Ly, dims->Lz, ops[i].momentum, &momentum[i * vol]);
+    std::vector<int> tlist;
+    if (ts)
+      tlist.assign(ts, ts + n_ts);
+    else
+      for (int t = 0; t < dims->Lt; ++t) tlist.push_back(t);
+    size_t const blk = static_cast<size_t>(nev) * nev;
+    std::string err;
+#pragma omp parallel num_threads(oracle_threads())
+    {
+      std::vector<cd> W(static_cast<size_t>(dim_row) * nev);
+#pragma omp for schedule(dynamic)
+      for (size_t it = 0; it < tlist.size(); ++it) {
+        int const t = tlist[it];
+        cd const *Vt = reinterpret_cast<cd const *>(V[t]);
+        for (int o = 0; o < n_ops; ++o) {
+          cd *dst = reinterpret_cast<cd *>(out) + (static_cast<size_t>(o) * dims->Lt + t) * blk;
+          if (ops[o].id != index_of_unity) {
+            // W = diag(mom) V with mom(x) = momentum[x / 3] (:292-297)
+            cd const *mom = &momentum[ops[o].id * vol];
+            for (int j = 0; j < nev; ++j)
+              for (long x = 0; x < dim_row; ++x)
+                W[x + dim_row * j] = mul(mom[x / 3], Vt[x + dim_row * j]);
+            gemm_ah_b(Vt, W.data(), dim_row, nev, dst);  // :300
+          } else {
+            for (size_t i = 0; i < blk; ++i) dst[i] = 0;  // identity, :317
+            for (int i = 0; i < nev; ++i) dst[i + static_cast<size_t>(nev) * i] = 1.0;
+          }
+        }
+      }
+    }
+  });
+}
+
+int oracle_contract(const slaph_dims *dims, const slaph_plan *plan, const double *vdv,
+                    const double *const *peram, const double *noise, int accumulator,
+                    int single_block_pair, double *out) {
+  return guarded([&] {
+    check_dims(dims);
+    Inputs in{*dims, plan, vdv, peram, noise, plan->n_vdv_ops, accumulator == SLAPH_ACC_KAHAN};
+    DilScheme const ds(dims->Lt, dims->dilT, DilType::block);
+    int const n_bp = ds.size();
+    int const Lt = dims->Lt;
+
+    // Per block pair, the values of every (diagram, slice pair, request) in the
+    // order a single-threaded run of src/Correlators.cpp:86-116 produces them.
+    std::vector<std::vector<cd>> vals(n_bp);
+    std::vector<std::vector<std::pair<int, int>>> slices(n_bp);
+    for (int b = 0; b < n_bp; ++b) slices[b] = ds.slices(b);
+    std::string err;
+    bool failed = false;
+#pragma omp parallel num_threads(oracle_threads())
+    {
+      Parts q(in, ds);
+#pragma omp for schedule(dynamic)
+      for (int b = 0; b < n_bp; ++b) {
+        if (single_block_pair >= 0 && single_block_pair != b) continue;
+        bool stop;
+#pragma omp atomic read
+        stop = failed;
+        if (stop) continue;
+        try {
+          for (int d = 0; d < plan->n_diagrams; ++d) {
+            auto const &dg = plan->diagrams[d];
+            for (auto const &sp : slices[b])
+              for (int i = 0; i < dg.n_requests; ++i)
+                vals[b].push_back(resolve(dg.requests[i], sp.first, sp.second, q, in.kahan));
+          }
+        } catch (std::exception const &e) {
+#pragma omp critical(oracle_err)
+          {
+            failed = true;
+            err = e.what();
+          }
+        }
+        q.clear();
+      }
+    }
+    if (failed) throw std::runtime_error(err);
+
+    // Diagram::assemble / write (src/Diagram.cpp:96-147): per-request values
+    // summed per time difference, then divided by Lt.
+    long total = 0;
+    std::vector<long> offset(plan->n_diagrams);
+    for (int d = 0; d < plan->n_diagrams; ++d) {
+      offset[d] = total;
+      total += plan->diagrams[d].n_requests;
+    }
+    std::vector<cd> corr(static_cast<size_t>(total) * Lt, cd(0, 0));
+    for (int b = 0; b < n_bp; ++b) {
+      if (single_block_pair >= 0 && single_block_pair != b) continue;
+      size_t k = 0;
+      for (int d = 0; d < plan->n_diagrams; ++d) {
+        int const nr = plan->diagrams[d].n_requests;
+        for (auto const &sp : slices[b]) {
+          // get_time_delta, src/Correlators.cpp:21-23 (C++ % truncates).
+          int const dt = std::abs((sp.second - sp.first - Lt) % Lt);
+          for (int i = 0; i < nr; ++i) corr[(offset[d] + i) * Lt + dt] += vals[b][k++];
+        }
+      }
+    }
+    for (size_t i = 0; i < corr.size(); ++i) {
+      cd const v = corr[i] / static_cast<double>(Lt);
+      out[2 * i] = v.real();
+      out[2 * i + 1] = v.imag();
+    }
+  });
+}
+
+int oracle_read_eigenvectors(const char *path, long dim_row, int nev, double *out) {
+  return guarded([&] {
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) throw std::runtime_error("Eigenvector file does not exist!");
+    for (int c = 0; c < nev; ++c) {
+      size_t const n = std::fread(out + 2 * dim_row * c, sizeof(double), 2 * dim_row, fp);
+      if (n != static_cast<size_t>(2 * dim_row)) {
+        std::fclose(fp);
+        throw std::runtime_error("Problem while reading Eigenvectors!");
+      }
+    }
+    std::fclose(fp);
+  });
+}
+
+int oracle_read_perambulator(const char *path, int Lt, int nev, int dilT, int dilE, int dilD,
+                             double *out) {
+  return guarded([&] {
+    long const rows = 4L * nev * Lt;
+    long const cols = static_cast<long>(Lt / dilT) * dilE * dilD;
+    std::vector<cd> buf(static_cast<size_t>(rows) * cols);
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) throw std::runtime_error(std::string("failed to open file to read perambulator: ") + path);
+    size_t const n = std::fread(buf.data(), sizeof(cd), buf.size(), fp);
+    std::fclose(fp);
+    if (n != buf.size()) throw std::runtime_error("Failed to read perambulator.");
+    // Re-sort, src/Perambulator.cpp:53-64.
+    long const nb_inv = static_cast<long>(Lt) * dilE * dilD / dilT;
+    cd *P = reinterpret_cast<cd *>(out);
+    for (long i = 0; i < rows * cols; ++i) P[i] = 0;
+    for (long t1 = 0; t1 < Lt; ++t1)
+      for (long ev1 = 0; ev1 < nev; ++ev1)
+        for (long d1 = 0; d1 < 4; ++d1)
+          for (long t2 = 0; t2 < Lt / dilT; ++t2)
+            for (long ev2 = 0; ev2 < dilE; ++ev2)
+              for (long d2 = 0; d2 < dilD; ++d2) {
+                long const row_i = 4 * nev * t1 + 4 * ev1 + d1;
+                long const col_i = dilD * dilE * t2 + dilD * ev2 + d2;
+                long const r = 4 * nev * t1 + nev * d1 + ev1;
+                long const c = dilE * dilD * t2 + dilE * d2 + ev2;
+                P[r + rows * c] = buf[row_i * nb_inv + col_i];
+              }
+  });
+}
+
+int oracle_read_random_vector(const char *path, long length, double *out) {
+  return guarded([&] {
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) throw std::runtime_error(std::string("failed to open file to read random vector: ") + path);
+    size_t const n = std::fread(out, sizeof(cd), length, fp);
+    std::fclose(fp);
+    if (n != static_cast<size_t>(length))
+      throw std::runtime_error("It seems that not all data are read from random vector file");
+  });
+}
+
+long oracle_dilution_text(int num_slice, int num_block, int type, char *buf, long len) {
+  std::string s;
+  char line[256];
+  DilType const ty = type == 0 ? DilType::block : DilType::interlace;
+  char const *name = type == 0 ? "B" : "I";
+  int const block_size = num_slice / num_block;
+  std::snprintf(line, sizeof line, "T = %d, T%s%d (Morningstar), T%s%d (Other):\n\n", num_slice,
+                name, num_block, name, block_size);
+  s += line;
+  DilScheme ds(num_slice, block_size, ty);
+  for (int b = 0; b < ds.size(); ++b) {
+    auto bl = ds.blocks(b);
+    std::snprintf(line, sizeof line, "%2d => %2d\n", bl.first, bl.second);
+    s += line;
+    for (auto const &sp : ds.slices(b)) {
+      std::snprintf(line, sizeof line, "  %2d -> %2d\n", sp.first, sp.second);
+      s += line;
+    }
+  }
+  s += "\n\n";
+  if (buf && len > 0) {
+    std::strncpy(buf, s.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return static_cast<long>(s.size()) + 1;
+}
+
+double oracle_kahan_sum(const double *xs, long n) {
+  double sum = 0, c = 0;
+  for (long i = 0; i < n; ++i) {
+    double const t = sum + xs[i];
+    if (std::abs(sum) >= std::abs(xs[i]))
+      c += (sum - t) + xs[i];
+    else
+      c += (xs[i] - t) + sum;
+    sum = t;
+  }
+  return sum + c;
+}
+
+}  // extern "C"

@@ -1,0 +1,174 @@
+// C ABI of the host-only parts: errors, front end, readers, HDF5 writer.
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "capi_util.hpp"
+#include "frontend.hpp"
+
+namespace slaph {
+namespace {
+thread_local std::string g_last_error;
+}
+void set_last_error(std::string const &m) { g_last_error = m; }
+}  // namespace slaph
+
+struct slaph_frontend {
+  slaph::GlobalData gd;
+  std::unique_ptr<slaph::FlatPlan> plan;
+};
+
+namespace {
+void copy_str(std::string const &s, char *buf, size_t len) {
+  if (!buf || len == 0) throw slaph::ArgError("null buffer");
+  if (s.size() + 1 > len) throw slaph::ArgError("buffer too small for '" + s + "'");
+  std::memcpy(buf, s.c_str(), s.size() + 1);
+}
+}  // namespace
+
+extern "C" {
+
+const char *slaph_last_error(void) { return slaph::g_last_error.c_str(); }
+
+int slaph_trace_kind_arity(int kind) { return slaph::trace_kind_arity(kind); }
+const char *slaph_trace_kind_name(int kind) { return slaph::trace_kind_name(kind); }
+
+int slaph_frontend_create(const char *infile_path, int argc, const char *const *argv,
+                          slaph_frontend **out) {
+  return slaph::guarded(
+      [&] {
+        if (!infile_path || !out) throw slaph::ArgError("null argument");
+        *out = nullptr;
+        auto fe = std::make_unique<slaph_frontend>();
+        std::vector<std::string> args;
+        for (int i = 0; i < argc; ++i) args.emplace_back(argv[i] ? argv[i] : "");
+        slaph::read_parameters(fe->gd, infile_path, args);
+        fe->plan = std::make_unique<slaph::FlatPlan>(fe->gd);
+        *out = fe.release();
+      },
+      SLAPH_ERR_PARSE);
+}
+
+int slaph_frontend_destroy(slaph_frontend *fe) {
+  delete fe;
+  return SLAPH_OK;
+}
+
+int slaph_frontend_dims(const slaph_frontend *fe, slaph_dims *out) {
+  return slaph::guarded([&] {
+    if (!fe || !out) throw slaph::ArgError("null argument");
+    auto const &gd = fe->gd;
+    if (gd.quarks.empty()) throw slaph::ArgError("no quarks defined");
+    slaph_dims d{};
+    d.Lt = gd.Lt;
+    d.Lx = gd.Lx;
+    d.Ly = gd.Ly;
+    d.Lz = gd.Lz;
+    d.nev = gd.number_of_eigen_vec;
+    d.dilT = gd.quarks[0].number_of_dilution_T;
+    d.dilE = gd.quarks[0].number_of_dilution_E;
+    int n = 0;
+    for (auto const &q : gd.quarks) n += q.number_of_rnd_vec;
+    d.n_rnd = n;
+    *out = d;
+  });
+}
+
+int slaph_frontend_plan(const slaph_frontend *fe, const slaph_plan **out) {
+  return slaph::guarded([&] {
+    if (!fe || !out) throw slaph::ArgError("null argument");
+    *out = &fe->plan->plan();
+  });
+}
+
+int slaph_frontend_get_int(const slaph_frontend *fe, const char *key, int64_t *out) {
+  return slaph::guarded([&] {
+    if (!fe || !key || !out) throw slaph::ArgError("null argument");
+    auto const &gd = fe->gd;
+    std::string const k = key;
+    if (k == "start_config")
+      *out = gd.start_config;
+    else if (k == "end_config")
+      *out = gd.end_config;
+    else if (k == "delta_config")
+      *out = gd.delta_config;
+    else if (k == "single_time_slice_combination")
+      *out = gd.single_time_slice_combination;
+    else if (k == "n_quarks")
+      *out = static_cast<int64_t>(gd.quarks.size());
+    else if (k == "nb_eigen_threads")
+      *out = gd.nb_eigen_threads;
+    else
+      throw slaph::ArgError("unknown integer setting '" + k + "'");
+  });
+}
+
+int slaph_frontend_get_str(const slaph_frontend *fe, const char *key, char *buf, size_t len) {
+  return slaph::guarded([&] {
+    if (!fe || !key) throw slaph::ArgError("null argument");
+    auto const &gd = fe->gd;
+    std::string const k = key;
+    if (k == "output_path")
+      copy_str(gd.path_output, buf, len);
+    else if (k == "path_eigenvectors")
+      copy_str(gd.path_eigenvectors, buf, len);
+    else if (k == "name_eigenvectors")
+      copy_str(gd.name_eigenvectors, buf, len);
+    else if (k == "handling_vdaggerv")
+      copy_str(gd.handling_vdaggerv, buf, len);
+    else if (k == "path_vdaggerv")
+      copy_str(gd.path_vdaggerv, buf, len);
+    else if (k == "path_config")
+      copy_str(gd.path_config, buf, len);
+    else
+      throw slaph::ArgError("unknown string setting '" + k + "'");
+  });
+}
+
+int slaph_frontend_io_name(const slaph_frontend *fe, int config, int which, int index, char *buf,
+                           size_t len) {
+  return slaph::guarded([&] {
+    if (!fe) throw slaph::ArgError("null argument");
+    copy_str(slaph::io_name(fe->gd, config, which, index), buf, len);
+  });
+}
+
+int slaph_read_eigenvectors(const char *path, int64_t dim_row, int32_t nev, double *out) {
+  return slaph::guarded([&] {
+    if (!path || !out || dim_row < 1 || nev < 1) throw slaph::ArgError("invalid argument");
+    slaph::read_eigenvectors(path, dim_row, nev, out);
+  });
+}
+
+int slaph_read_perambulator(const char *path, int32_t Lt, int32_t nev, int32_t dilT, int32_t dilE,
+                            int32_t dilD, double *out) {
+  return slaph::guarded([&] {
+    if (!path || !out) throw slaph::ArgError("invalid argument");
+    slaph::read_perambulator(path, Lt, nev, dilT, dilE, dilD, out);
+  });
+}
+
+int slaph_read_random_vector(const char *path, int64_t length, double *out) {
+  return slaph::guarded([&] {
+    if (!path || !out || length < 1) throw slaph::ArgError("invalid argument");
+    slaph::read_random_vector(path, length, out);
+  });
+}
+
+int slaph_write_correlators_h5(const char *file_path, int32_t n_datasets,
+                               const char *const *dataset_names, int32_t Lt, const double *data) {
+  return slaph::guarded([&] {
+    if (!file_path) throw slaph::ArgError("null path");
+    slaph::write_correlators_h5(file_path, n_datasets, dataset_names, Lt, data);
+  });
+}
+
+int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt) {
+  if (!plan || Lt < 1) return -1;
+  int64_t n = 0;
+  for (int32_t d = 0; d < plan->n_diagrams; ++d) n += plan->diagrams[d].n_requests;
+  return n * Lt * 2;
+}
+
+}  // extern "C"

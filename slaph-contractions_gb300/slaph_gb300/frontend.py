@@ -1,0 +1,142 @@
+"""Python mirror of the reference front end (GlobalData + read_parameters).
+
+``GlobalData.from_infile`` parses a reference infile through the C ABI
+(slaph_frontend_*) and exposes the lookup tables both as the flat C plan the
+engine consumes and as plain Python structures for inspection.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+@dataclass
+class FactorIndex:
+    id_vdaggerv: int
+    need_vdaggerv_daggering: bool
+    gamma: int
+    rnd_vec_ids: list
+
+
+@dataclass
+class TraceRequest:
+    tr_name: str
+    tr_id: int
+    locations: list  # "source" / "sink"
+
+
+@dataclass
+class CorrelatorRequest:
+    trace_requests: list
+    hdf5_dataset_name: str
+
+
+class GlobalData:
+    """Parsed infile plus lookup tables (include/global_data.hpp:104-160)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        d = L.Dims()
+        L.check(L.lib().slaph_frontend_dims(self._h, C.byref(d)))
+        self.dims = d
+        p = C.POINTER(L.Plan)()
+        L.check(L.lib().slaph_frontend_plan(self._h, C.byref(p)))
+        self.plan_ptr = p
+
+    @classmethod
+    def from_infile(cls, path, args=()):
+        argv = (C.c_char_p * max(1, len(args)))(*[a.encode() for a in args])
+        h = C.c_void_p()
+        L.check(L.lib().slaph_frontend_create(str(path).encode(), len(args), argv, C.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if self._h:
+            L.lib().slaph_frontend_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_int(self, key):
+        v = C.c_int64()
+        L.check(L.lib().slaph_frontend_get_int(self._h, key.encode(), C.byref(v)))
+        return v.value
+
+    def get_str(self, key):
+        buf = C.create_string_buffer(4096)
+        L.check(L.lib().slaph_frontend_get_str(self._h, key.encode(), buf, 4096))
+        return buf.value.decode()
+
+    def io_name(self, config, which, index=0):
+        buf = C.create_string_buffer(4096)
+        L.check(L.lib().slaph_frontend_io_name(self._h, config, which, index, buf, 4096))
+        return buf.value.decode()
+
+    # -- views of the lookup tables -------------------------------------
+    @property
+    def plan(self):
+        return self.plan_ptr.contents
+
+    def vdaggerv_lookup(self):
+        p = self.plan
+        out = []
+        for i in range(p.n_vdv_ops):
+            o = p.vdv_ops[i]
+            disp = o.disp[:2 * o.n_disp].decode() if o.n_disp else ""
+            out.append((o.id, tuple(o.momentum), disp))
+        return out
+
+    def quarkline_lookuptable(self):
+        p = self.plan
+        out = {}
+        for q, name in enumerate(("Q0", "Q1", "Q2")):
+            lst = []
+            for i in range(p.n_factors[q]):
+                f = p.factors[q][i]
+                pairs = [(f.rnd_pairs[2 * k], f.rnd_pairs[2 * k + 1]) for k in range(f.n_rnd_pairs)]
+                lst.append(FactorIndex(f.id_vdaggerv, bool(f.need_vdaggerv_daggering), f.gamma, pairs))
+            out[name] = lst
+        return out
+
+    def trace_indices_map(self):
+        p = self.plan
+        out = {}
+        for k, name in enumerate(L.TRACE_KINDS):
+            ar = L.TRACE_ARITY[k]
+            n = p.n_trace_ids[k]
+            ids = np.ctypeslib.as_array(p.trace_ql_ids[k], shape=(n * ar,)) if n else np.zeros(0, int)
+            out[name] = [list(map(int, ids[i * ar:(i + 1) * ar])) for i in range(n)]
+        return out
+
+    def correlator_requests_map(self):
+        p = self.plan
+        out = {}
+        for d in range(p.n_diagrams):
+            dg = p.diagrams[d]
+            reqs = []
+            for i in range(dg.n_requests):
+                r = dg.requests[i]
+                trs = []
+                for j in range(r.n_traces):
+                    t = r.traces[j]
+                    locs = ["source" if t.loc[m] == 0 else "sink" for m in range(t.n_loc)]
+                    trs.append(TraceRequest(L.TRACE_KINDS[t.kind], t.tr_id, locs))
+                reqs.append(CorrelatorRequest(trs, r.dataset_name.decode()))
+            out[dg.name.decode()] = reqs
+        return out
+
+    def output_layout(self):
+        """[(diagram name, [dataset names])] in the order contract() writes them."""
+        return [(name, [r.hdf5_dataset_name for r in reqs])
+                for name, reqs in self.correlator_requests_map().items()]
+
+    def output_doubles(self):
+        return int(L.lib().slaph_plan_output_doubles(self.plan_ptr, self.dims.Lt))
