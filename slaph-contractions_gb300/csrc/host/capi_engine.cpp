@@ -1,0 +1,86 @@
+// C ABI of the engine (include/slaph_gb300.h).
+#include <memory>
+
+#include "capi_util.hpp"
+#include "engine.hpp"
+
+struct slaph_engine {
+  std::unique_ptr<slaph::Engine> e;
+};
+
+namespace {
+slaph::Engine &get(slaph_engine *eng) {
+  if (!eng || !eng->e) throw slaph::ArgError("null engine");
+  return *eng->e;
+}
+}  // namespace
+
+extern "C" {
+
+int slaph_engine_create(const slaph_dims *dims, slaph_engine **out) {
+  return slaph::guarded([&] {
+    if (!dims || !out) throw slaph::ArgError("null argument");
+    *out = nullptr;
+    auto eng = std::make_unique<slaph_engine>();
+    eng->e = std::make_unique<slaph::Engine>(*dims);
+    *out = eng.release();
+  });
+}
+
+int slaph_engine_destroy(slaph_engine *eng) {
+  delete eng;
+  return SLAPH_OK;
+}
+
+int slaph_engine_set_operators(slaph_engine *eng, const slaph_vdv_op *ops, int32_t n_ops,
+                               int32_t index_of_unity) {
+  return slaph::guarded([&] { get(eng).set_operators(ops, n_ops, index_of_unity); });
+}
+
+int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V) {
+  return slaph::guarded([&] { get(eng).set_eigenvectors(t, V); });
+}
+
+int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram) {
+  return slaph::guarded([&] { get(eng).set_perambulator(rnd_id, peram); });
+}
+
+int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise) {
+  return slaph::guarded([&] { get(eng).set_random_vector(rnd_id, noise); });
+}
+
+int slaph_vdaggerv_build(slaph_engine *eng, int precision) {
+  return slaph::guarded([&] { get(eng).vdaggerv_build(precision); });
+}
+
+int slaph_vdaggerv_fetch(slaph_engine *eng, int32_t op_id, int32_t t, double *out) {
+  return slaph::guarded([&] { get(eng).vdaggerv_fetch(op_id, t, out); });
+}
+
+int slaph_contract(slaph_engine *eng, const slaph_plan *plan, int precision, int accumulator,
+                   int single_block_pair, double *corr_out) {
+  return slaph::guarded(
+      [&] { get(eng).contract(plan, precision, accumulator, single_block_pair, corr_out); });
+}
+
+int slaph_engine_timings(const slaph_engine *eng, double *out, int n) {
+  if (!eng || !eng->e || !out || n < 0) {
+    slaph::set_last_error("invalid argument");
+    return -1;
+  }
+  int const m = n < 6 ? n : 6;
+  for (int i = 0; i < m; ++i) out[i] = eng->e->timings[i];
+  return m;
+}
+
+int slaph_engine_stats(const slaph_engine *eng, double *out, int n) {
+  if (!eng || !eng->e || !out || n < 0) {
+    slaph::set_last_error("invalid argument");
+    return -1;
+  }
+  int const m = n < 6 ? n : 6;
+  for (int i = 0; i < m; ++i) out[i] = eng->e->stats[i];
+  return m;
+}
+
+}  // extern "C"

@@ -1,0 +1,384 @@
+// Engine host logic: device memory, schedule upload, kernel sequencing.
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+namespace slaph {
+
+static_assert(sizeof(Q0MInst) == sizeof(dev::Q0MInst), "layout");
+static_assert(sizeof(Q1RInst) == sizeof(dev::Q1RInst), "layout");
+static_assert(sizeof(Q2MInst) == sizeof(dev::Q2MInst), "layout");
+static_assert(sizeof(Q0Inst) == sizeof(dev::Q0Inst), "layout");
+static_assert(sizeof(Q1Inst) == sizeof(dev::Q1Inst), "layout");
+static_assert(sizeof(Q2Inst) == sizeof(dev::Q2Inst), "layout");
+static_assert(sizeof(ProdInst) == sizeof(dev::ProdInst), "layout");
+static_assert(sizeof(TraceList) == sizeof(dev::TraceList), "layout");
+static_assert(sizeof(Term) == sizeof(dev::Term), "layout");
+
+void cuda_check(cudaError_t e, char const *what) {
+  if (e == cudaSuccess) return;
+  std::string const msg = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) throw NoMemError(msg);
+  throw CudaError(msg);
+}
+
+void DevBuf::reserve(size_t bytes) {
+  if (bytes <= n_) return;
+  release();
+  if (bytes == 0) return;
+  cudaError_t const e = cudaMalloc(&p_, bytes);
+  if (e != cudaSuccess) {
+    p_ = nullptr;
+    (void)cudaGetLastError();
+    throw NoMemError("device allocation of " + std::to_string(bytes) + " bytes failed: " +
+                     cudaGetErrorString(e));
+  }
+  n_ = bytes;
+}
+
+void DevBuf::release() {
+  if (p_) cudaFree(p_);
+  p_ = nullptr;
+  n_ = 0;
+}
+
+namespace {
+
+template <typename T>
+void upload(DevBuf &b, std::vector<T> const &v, cudaStream_t s) {
+  b.reserve(std::max<size_t>(1, v.size()) * sizeof(T));
+  if (!v.empty())
+    SLAPH_CK(cudaMemcpyAsync(b.as<void>(), v.data(), v.size() * sizeof(T),
+                             cudaMemcpyHostToDevice, s));
+}
+
+double elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  SLAPH_CK(cudaEventElapsedTime(&ms, a, b));
+  return ms;
+}
+
+}  // namespace
+
+Engine::Engine(slaph_dims const &d) : dims_(d) {
+  if (d.Lt < 1 || d.Lx < 1 || d.Ly < 1 || d.Lz < 1 || d.nev < 1 || d.dilT < 1 || d.dilE < 1 ||
+      d.n_rnd < 1)
+    throw ArgError("invalid slaph_dims: every size must be positive");
+  if (d.Lt % d.dilT != 0) throw ArgError("Lt must be a multiple of dilT");
+  if (d.n_rnd > 16) throw UnsupportedError("at most 16 random vectors (16-bit used masks)");
+  if (4 * d.dilE > 64) throw UnsupportedError("4*dilE above 64 is not supported");
+  geo_.Lt = d.Lt;
+  geo_.Lx = d.Lx;
+  geo_.Ly = d.Ly;
+  geo_.Lz = d.Lz;
+  geo_.nev = d.nev;
+  geo_.dilE = d.dilE;
+  geo_.n_rnd = d.n_rnd;
+  geo_.nb = d.Lt / d.dilT;
+  geo_.dim_row = 3LL * d.Lx * d.Ly * d.Lz;
+  SLAPH_CK(cudaGetDevice(&device_));
+  SLAPH_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  for (auto &e : ev_) SLAPH_CK(cudaEventCreate(&e));
+  V_.reserve(sizeof(double2) * geo_.dim_row * d.nev * d.Lt);
+  peram_.reserve(sizeof(double2) * peram_elems() * d.n_rnd);
+  noise_.reserve(sizeof(double2) * 4LL * d.nev * d.Lt * d.n_rnd);
+  SLAPH_CK(cudaMemsetAsync(noise_.as<void>(), 0, noise_.size(), stream_));
+  SLAPH_CK(cudaMemsetAsync(peram_.as<void>(), 0, peram_.size(), stream_));
+  SLAPH_CK(dev::upload_gamma(stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+}
+
+Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (auto &e : ev_)
+    if (e) cudaEventDestroy(e);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+int64_t Engine::peram_elems() const {
+  return 4LL * dims_.nev * dims_.Lt * (dims_.Lt / dims_.dilT) * dims_.dilE * 4;
+}
+
+void Engine::set_operators(slaph_vdv_op const *ops, int32_t n, int32_t index_of_unity) {
+  if (n < 0 || (n > 0 && !ops)) throw ArgError("invalid operator list");
+  for (int32_t i = 0; i < n; ++i) {
+    if (ops[i].id != i) throw ArgError("VdaggerV ids must be 0..n_ops-1 in order");
+    if (ops[i].n_disp != 0)
+      throw UnsupportedError(
+          "displaced operators (covariant derivative VdaggerV) are not supported by this "
+          "engine");
+  }
+  if (index_of_unity >= n) throw ArgError("index_of_unity out of range");
+  ops_.assign(ops, ops + n);
+  index_of_unity_ = index_of_unity;
+  std::vector<int32_t> mom(3 * std::max(n, 1), 0);
+  for (int32_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) mom[3 * i + c] = ops[i].momentum[c];
+  upload(mom_dev_, mom, stream_);
+  int64_t const vol = geo_.dim_row / 3;
+  phase_.reserve(sizeof(double2) * vol * std::max(n, 1));
+  launch(dev::momenta(phase_.as<double2>(), mom_dev_.as<int32_t>(), n, geo_, stream_),
+         "momenta");
+  vdv_.reserve(sizeof(double2) * 2LL * std::max(n, 1) * dims_.Lt * dims_.nev * dims_.nev);
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  ops_set_ = true;
+  vdv_built_ = false;
+}
+
+void Engine::set_eigenvectors(int32_t t, double const *V) {
+  if (t < 0 || t >= dims_.Lt || !V) throw ArgError("invalid timeslice or null pointer");
+  size_t const n = static_cast<size_t>(geo_.dim_row) * dims_.nev;
+  SLAPH_CK(cudaMemcpyAsync(V_.as<double2>() + n * t, V, n * sizeof(double2),
+                           cudaMemcpyHostToDevice, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  vdv_built_ = false;
+}
+
+void Engine::set_perambulator(int32_t r, double const *P) {
+  if (r < 0 || r >= dims_.n_rnd || !P) throw ArgError("invalid random vector index");
+  size_t const n = static_cast<size_t>(peram_elems());
+  SLAPH_CK(cudaMemcpyAsync(peram_.as<double2>() + n * r, P, n * sizeof(double2),
+                           cudaMemcpyHostToDevice, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+}
+
+void Engine::set_random_vector(int32_t r, double const *noise) {
+  if (r < 0 || r >= dims_.n_rnd || !noise) throw ArgError("invalid random vector index");
+  size_t const n = 4ULL * dims_.nev * dims_.Lt;
+  SLAPH_CK(cudaMemcpyAsync(noise_.as<double2>() + n * r, noise, n * sizeof(double2),
+                           cudaMemcpyHostToDevice, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+}
+
+void Engine::vdaggerv_build(int precision) {
+  if (!ops_set_) throw StateError("slaph_engine_set_operators must be called first");
+  if (precision != SLAPH_FP64 && precision != SLAPH_MIXED)
+    throw ArgError("unknown precision mode");
+  if (precision == SLAPH_MIXED)
+    throw UnsupportedError("the split-precision VdaggerV path is not available in this build");
+  launches_ = 0;
+  std::vector<int32_t> computed;
+  for (auto const &o : ops_)
+    if (o.id != index_of_unity_) computed.push_back(o.id);
+  DevBuf list;
+  upload(list, computed, stream_);
+  SLAPH_CK(cudaEventRecord(ev_[0], stream_));
+  launch(dev::vdaggerv_fp64(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
+                            list.as<int32_t>(), static_cast<int32_t>(computed.size()), 0,
+                            dims_.Lt, geo_, stream_),
+         "vdaggerv_fp64");
+  if (index_of_unity_ >= 0)
+    launch(dev::vdaggerv_identity(vdv_.as<double2>(), index_of_unity_, geo_, stream_),
+           "vdaggerv_identity");
+  launch(dev::vdaggerv_daggers(vdv_.as<double2>(), static_cast<int32_t>(ops_.size()), geo_,
+                               stream_),
+         "vdaggerv_daggers");
+  SLAPH_CK(cudaEventRecord(ev_[1], stream_));
+  SLAPH_CK(cudaEventSynchronize(ev_[1]));
+  timings[0] = elapsed_ms(ev_[0], ev_[1]);
+  timings[5] = static_cast<double>(launches_);
+  vdv_built_ = true;
+}
+
+void Engine::vdaggerv_fetch(int32_t op, int32_t t, double *out) {
+  if (!vdv_built_) throw StateError("VdaggerV has not been built");
+  if (op < 0 || op >= static_cast<int32_t>(ops_.size()) || t < 0 || t >= dims_.Lt || !out)
+    throw ArgError("invalid operator id or timeslice");
+  size_t const blk = static_cast<size_t>(dims_.nev) * dims_.nev;
+  SLAPH_CK(cudaMemcpyAsync(out, vdv_.as<double2>() + (2ULL * op * dims_.Lt + t) * blk,
+                           blk * sizeof(double2), cudaMemcpyDeviceToHost, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+}
+
+void Engine::prepare_schedule(slaph_plan const *plan, int bp) {
+  if (sched_ && sched_plan_ == plan && sched_bp_ == bp) return;
+  sched_.reset();
+  auto const t0 = std::chrono::steady_clock::now();
+  auto ds = std::make_unique<DeviceSchedule>();
+  ds->s = build_schedule(dims_, *plan, bp);
+  Schedule const &s = ds->s;
+  upload(ds->q0m, s.q0m, stream_);
+  upload(ds->q1r, s.q1r, stream_);
+  upload(ds->q2m, s.q2m, stream_);
+  upload(ds->q0, s.q0, stream_);
+  upload(ds->q1, s.q1, stream_);
+  upload(ds->q2, s.q2, stream_);
+  std::vector<int64_t> off{0};
+  std::vector<int32_t> si, sj;
+  std::vector<uint16_t> sm;
+  for (auto const &sh : s.shapes) {
+    si.insert(si.end(), sh.i.begin(), sh.i.end());
+    sj.insert(sj.end(), sh.j.begin(), sh.j.end());
+    sm.insert(sm.end(), sh.mask.begin(), sh.mask.end());
+    off.push_back(static_cast<int64_t>(si.size()));
+  }
+  upload(ds->shape_i, si, stream_);
+  upload(ds->shape_j, sj, stream_);
+  upload(ds->shape_mask, sm, stream_);
+  upload(ds->shape_off, off, stream_);
+  int64_t const Lt = dims_.Lt;
+  for (auto const &w : s.waves) {
+    auto wb = std::make_unique<DeviceSchedule::WaveBufs>();
+    upload(wb->prods, w.prods, stream_);
+    upload(wb->lists, w.lists, stream_);
+    upload(wb->terms, w.terms, stream_);
+    // Stable counting sort of the terms by output (request, dt) gives the
+    // per-output summation order of Diagram::assemble.
+    int64_t const n_out = s.n_outputs * Lt;
+    std::vector<int64_t> count(n_out + 1, 0);
+    for (auto const &t : w.terms) ++count[t.out * Lt + t.dt + 1];
+    std::vector<int32_t> seg_out;
+    std::vector<int64_t> seg_off{0};
+    std::vector<int64_t> start(n_out, 0);
+    int64_t acc = 0;
+    for (int64_t o = 0; o < n_out; ++o) {
+      start[o] = acc;
+      if (count[o + 1]) {
+        seg_out.push_back(static_cast<int32_t>(o));
+        acc += count[o + 1];
+        seg_off.push_back(acc);
+      }
+    }
+    std::vector<int32_t> idx(w.terms.size());
+    for (size_t k = 0; k < w.terms.size(); ++k) {
+      auto const &t = w.terms[k];
+      idx[start[t.out * Lt + t.dt]++] = static_cast<int32_t>(k);
+    }
+    wb->n_seg = static_cast<int64_t>(seg_out.size());
+    upload(wb->seg_out, seg_out, stream_);
+    upload(wb->seg_off, seg_off, stream_);
+    upload(wb->idx, idx, stream_);
+    SLAPH_CK(cudaStreamSynchronize(stream_));
+    ds->waves.push_back(std::move(wb));
+  }
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  ds->plan_seconds =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  sched_ = std::move(ds);
+  sched_plan_ = plan;
+  sched_bp_ = bp;
+}
+
+void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
+                      int single_block_pair, double *corr_out) {
+  if (!plan || !corr_out) throw ArgError("null plan or output");
+  if (!vdv_built_) throw StateError("slaph_vdaggerv_build must be called before contract");
+  if (precision != SLAPH_FP64 && precision != SLAPH_MIXED)
+    throw ArgError("unknown precision mode");
+  if (accumulator != SLAPH_ACC_NATIVE && accumulator != SLAPH_ACC_KAHAN)
+    throw ArgError("unknown accumulator");
+  if (plan->need_gaugefield)
+    throw UnsupportedError("displaced operators need a gauge field; not supported");
+  if (plan->n_vdv_ops != static_cast<int32_t>(ops_.size()))
+    throw ArgError("plan VdaggerV table does not match slaph_engine_set_operators");
+  for (int32_t d = 0; d < plan->n_diagrams; ++d)
+    if (plan->diagrams[d].n_requests > 0 && !plan->diagrams[d].requests)
+      throw ArgError("diagram without request array");
+  launches_ = 0;
+  auto const tp = std::chrono::steady_clock::now();
+  prepare_schedule(plan, single_block_pair);
+  double const plan_wall =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
+  DeviceSchedule &ds = *sched_;
+  Schedule const &s = ds.s;
+  int32_t const eds = s.eds;
+  int64_t const ms = static_cast<int64_t>(eds) * eds;
+  int64_t const nev = dims_.nev;
+
+  // ---- factors
+  SLAPH_CK(cudaEventRecord(ev_[0], stream_));
+  slots_.reserve(sizeof(double2) * ms * std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots));
+  {
+    DevBuf q0m, q1r, q2m;
+    q0m.reserve(sizeof(double2) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
+    q1r.reserve(sizeof(double2) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
+    q2m.reserve(sizeof(double2) * std::max<int64_t>(1, s.q2m.size()) * eds * 4 * nev);
+    double2 const *vdv = vdv_.as<double2>();
+    launch(dev::q0m(q0m.as<double2>(), ds.q0m.as<dev::Q0MInst>(), s.q0m.size(), vdv,
+                    noise_.as<double2>(), geo_, stream_),
+           "q0m");
+    launch(dev::q1r(q1r.as<double2>(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(), vdv,
+                    noise_.as<double2>(), geo_, stream_),
+           "q1r");
+    launch(dev::q2m(q2m.as<double2>(), ds.q2m.as<dev::Q2MInst>(), s.q2m.size(), vdv,
+                    peram_.as<double2>(), geo_, stream_),
+           "q2m");
+    launch(dev::q0(slots_.as<double2>(), ds.q0.as<dev::Q0Inst>(), s.q0.size(),
+                   q0m.as<double2>(), noise_.as<double2>(), geo_, stream_),
+           "q0");
+    launch(dev::q1(slots_.as<double2>(), ds.q1.as<dev::Q1Inst>(), s.q1.size(),
+                   q1r.as<double2>(), peram_.as<double2>(), geo_, stream_),
+           "q1");
+    launch(dev::q2(slots_.as<double2>(), ds.q2.as<dev::Q2Inst>(), s.q2.size(),
+                   q2m.as<double2>(), peram_.as<double2>(), geo_, stream_),
+           "q2");
+    SLAPH_CK(cudaEventRecord(ev_[1], stream_));
+    SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
+  }
+  timings[1] = elapsed_ms(ev_[0], ev_[1]);
+
+  // ---- waves: products, traces, terms, accumulation
+  values_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_values));
+  term_val_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_terms));
+  int64_t const n_run = std::max<int64_t>(1, s.n_outputs * dims_.Lt);
+  running_.reserve(sizeof(double2) * n_run);
+  SLAPH_CK(cudaMemsetAsync(running_.as<void>(), 0, sizeof(double2) * n_run, stream_));
+  double t_pt = 0, t_as = 0;
+  for (size_t wi = 0; wi < s.waves.size(); ++wi) {
+    Wave const &w = s.waves[wi];
+    auto &wb = *ds.waves[wi];
+    SLAPH_CK(cudaEventRecord(ev_[2], stream_));
+    auto const *prods = wb.prods.as<dev::ProdInst>();
+    for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
+      int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
+      if (e > b)
+        launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
+    }
+    launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
+                       static_cast<int64_t>(w.lists.size()), ds.shape_i.as<int32_t>(),
+                       ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
+                       slots_.as<double2>(), eds, w.n_values, stream_),
+           "traces");
+    SLAPH_CK(cudaEventRecord(ev_[3], stream_));
+    launch(dev::terms(term_val_.as<double2>(), wb.terms.as<dev::Term>(),
+                      static_cast<int64_t>(w.terms.size()), wb.lists.as<dev::TraceList>(),
+                      values_.as<double2>(), ds.shape_mask.as<uint16_t>(),
+                      ds.shape_off.as<int64_t>(), accumulator == SLAPH_ACC_KAHAN ? 1 : 0,
+                      stream_),
+           "terms");
+    launch(dev::accumulate(running_.as<double2>(), wb.seg_out.as<int32_t>(),
+                           wb.seg_off.as<int64_t>(), wb.n_seg, wb.idx.as<int32_t>(),
+                           term_val_.as<double2>(), stream_),
+           "accumulate");
+    SLAPH_CK(cudaEventRecord(ev_[4], stream_));
+    SLAPH_CK(cudaEventSynchronize(ev_[4]));
+    t_pt += elapsed_ms(ev_[2], ev_[3]);
+    t_as += elapsed_ms(ev_[3], ev_[4]);
+  }
+  timings[2] = t_pt;
+  timings[3] = t_as;
+  timings[4] = plan_wall * 1e3;
+  timings[5] = static_cast<double>(launches_);
+
+  // ---- output: C[t] = correlator[t][i] / Lt (src/Diagram.cpp:141-143)
+  std::vector<double2> host(static_cast<size_t>(s.n_outputs * dims_.Lt));
+  if (!host.empty())
+    SLAPH_CK(cudaMemcpyAsync(host.data(), running_.as<double2>(), host.size() * sizeof(double2),
+                             cudaMemcpyDeviceToHost, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  double const inv = static_cast<double>(dims_.Lt);
+  for (size_t i = 0; i < host.size(); ++i) {
+    corr_out[2 * i] = host[i].x / inv;
+    corr_out[2 * i + 1] = host[i].y / inv;
+  }
+  stats[0] = static_cast<double>(s.q0.size() + s.q1.size() + s.q2.size());
+  stats[1] = static_cast<double>(s.n_prods);
+  stats[2] = static_cast<double>(s.n_trace_entries);
+  stats[3] = static_cast<double>(s.n_terms);
+  stats[4] = s.flops_factors;
+  stats[5] = s.flops_products + s.flops_traces;
+}
+
+}  // namespace slaph

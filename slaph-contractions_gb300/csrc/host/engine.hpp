@@ -1,0 +1,100 @@
+// Engine: device state for one lattice geometry and the per-configuration
+// calls of the hot path (VdaggerV build, contraction).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../../include/slaph_gb300.h"
+#include "../kernels/kernels.cuh"
+#include "capi_util.hpp"
+#include "schedule.hpp"
+
+namespace slaph {
+
+void cuda_check(cudaError_t e, char const *what);
+#define SLAPH_CK(call) ::slaph::cuda_check((call), #call)
+
+// Owning device allocation.
+class DevBuf {
+ public:
+  DevBuf() = default;
+  ~DevBuf() { release(); }
+  DevBuf(DevBuf const &) = delete;
+  DevBuf &operator=(DevBuf const &) = delete;
+  void reserve(size_t bytes);  // grows, never shrinks; contents undefined
+  void release();
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(p_);
+  }
+  size_t size() const { return n_; }
+
+ private:
+  void *p_ = nullptr;
+  size_t n_ = 0;
+};
+
+// A schedule plus its work lists resident on the device.
+struct DeviceSchedule {
+  Schedule s;
+  DevBuf q0m, q1r, q2m, q0, q1, q2;
+  DevBuf shape_i, shape_j, shape_mask, shape_off;
+  struct WaveBufs {
+    DevBuf prods, lists, terms, seg_out, seg_off, idx;
+    int64_t n_seg = 0;
+  };
+  std::vector<std::unique_ptr<WaveBufs>> waves;
+  double plan_seconds = 0;
+};
+
+class Engine {
+ public:
+  explicit Engine(slaph_dims const &dims);
+  ~Engine();
+
+  void set_operators(slaph_vdv_op const *ops, int32_t n, int32_t index_of_unity);
+  void set_eigenvectors(int32_t t, double const *V);
+  void set_perambulator(int32_t r, double const *peram);
+  void set_random_vector(int32_t r, double const *noise);
+  void vdaggerv_build(int precision);
+  void vdaggerv_fetch(int32_t op, int32_t t, double *out);
+  void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
+                double *corr_out);
+
+  double timings[6] = {0, 0, 0, 0, 0, 0};
+  double stats[6] = {0, 0, 0, 0, 0, 0};
+
+ private:
+  slaph_dims dims_;
+  dev::Geometry geo_{};
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev_[8] = {};
+
+  DevBuf V_, peram_, noise_, phase_, vdv_, ops_dev_, mom_dev_;
+  std::vector<slaph_vdv_op> ops_;
+  int32_t index_of_unity_ = -1;
+  bool ops_set_ = false, vdv_built_ = false;
+  int64_t launches_ = 0;
+
+  // Working buffers of the contraction.
+  DevBuf slots_, values_, term_val_, running_;
+
+  std::unique_ptr<DeviceSchedule> sched_;
+  slaph_plan const *sched_plan_ = nullptr;
+  int sched_bp_ = -2;
+
+  int64_t peram_elems() const;
+  void prepare_schedule(slaph_plan const *plan, int single_block_pair);
+  void launch(cudaError_t e, char const *what) {
+    cuda_check(e, what);
+    ++launches_;
+  }
+};
+
+}  // namespace slaph

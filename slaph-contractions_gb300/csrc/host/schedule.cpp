@@ -1,0 +1,498 @@
+// Symbolic replay of contract(): builds the flat work lists of schedule.hpp.
+#include "schedule.hpp"
+
+#include <algorithm>
+#include <cstdlib>
+#include <map>
+#include <tuple>
+#include <unordered_map>
+
+#include "capi_util.hpp"
+
+namespace slaph {
+
+namespace {
+
+// A DilutedFactor without data: random-vector pair and used-index mask.
+struct SymE {
+  int32_t r1, r2;
+  uint16_t used;
+  bool operator<(SymE const &o) const {
+    return std::tie(r1, r2, used) < std::tie(o.r1, o.r2, o.used);
+  }
+};
+
+// Concrete list: entry e lives in matrix slot base + e.  Product slots are
+// encoded as -(local + 1) until the factor slot count is final.
+struct ListRef {
+  int32_t shape;
+  int32_t base;
+  int32_t level;
+};
+
+struct ProdTemplate {
+  int32_t out_shape;
+  std::vector<std::pair<int32_t, int32_t>> pairs;
+};
+
+char const *const kMulEmpty =
+    "vector<DilutedFactor> operator*(vector<DilutedFactor>, vector<DilutedFactor>) has an "
+    "empty result.";
+char const *const kTrEmpty2 =
+    "vector<DilutedTrace> factor_to_trace(vector<DilutedFactor>, vector<DilutedFactor>) has an "
+    "empty result. Not enough random vectors?";
+char const *const kTrEmpty1 =
+    "vector<DilutedTrace> factor_to_trace(vector<DilutedFactor>) has an empty result.";
+char const *const kIpEmpty =
+    "compcomp_t inner_product(vector<DilutedTrace>, vector<DilutedTrace>) has an empty "
+    "result. Not enough random vectors?";
+
+inline uint64_t pack2(int64_t a, int64_t b) {
+  return (static_cast<uint64_t>(static_cast<uint32_t>(a)) << 32) | static_cast<uint32_t>(b);
+}
+
+class Builder {
+ public:
+  Builder(slaph_dims const &d, slaph_plan const &p) : dims_(d), plan_(p) {
+    s_.dims = d;
+    s_.eds = 4 * d.dilE;
+    s_.n_vdv = p.n_vdv_ops;
+    block_size_ = d.dilT;
+  }
+
+  Schedule run(int single_block_pair) {
+    int const Lt = dims_.Lt;
+    int const nb = Lt / block_size_;
+    int const n_bp = nb * (nb + 1) / 2;
+    std::vector<int64_t> offset(plan_.n_diagrams);
+    int64_t total = 0;
+    for (int d = 0; d < plan_.n_diagrams; ++d) {
+      offset[d] = total;
+      total += plan_.diagrams[d].n_requests;
+    }
+    s_.n_outputs = total;
+    for (int b = 0; b < n_bp; ++b) {
+      if (single_block_pair >= 0 && b != single_block_pair) continue;
+      begin_wave(b);
+      auto const slices = slice_pairs(b, nb);
+      for (int d = 0; d < plan_.n_diagrams; ++d) {
+        auto const &dg = plan_.diagrams[d];
+        for (auto const &sp : slices) {
+          int const dt = std::abs((sp.second - sp.first - Lt) % Lt);
+          for (int i = 0; i < dg.n_requests; ++i) {
+            auto const &req = dg.requests[i];
+            if (req.n_traces < 1 || req.n_traces > 3)
+              throw UnsupportedError("This many traces are not implemented yet.");
+            Term t{};
+            t.n = req.n_traces;
+            for (int k = 0; k < req.n_traces; ++k)
+              t.list[k] = trace_list(req.traces[k], sp.first, sp.second);
+            if (req.n_traces > 1) check_inner_product(t);
+            t.out = static_cast<int32_t>(offset[d] + i);
+            t.dt = dt;
+            w_.terms.push_back(t);
+          }
+        }
+      }
+      end_wave();
+    }
+    finish();
+    return std::move(s_);
+  }
+
+ private:
+  slaph_dims dims_;
+  slaph_plan const &plan_;
+  Schedule s_;
+  int block_size_;
+  int32_t n_factor_slots_ = 0;
+
+  std::vector<std::vector<SymE>> shapes_;
+  std::map<std::vector<SymE>, int32_t> shape_ids_;
+  std::unordered_map<uint64_t, int32_t> fshape_memo_;     // (type, ql) -> shape
+  std::unordered_map<uint64_t, int32_t> ptemplate_memo_;  // (shapeL, shapeR) -> template
+  std::vector<ProdTemplate> ptemplates_;
+  std::unordered_map<uint64_t, int32_t> tshape_memo_;     // (shapeL, shapeR|-1) -> trace shape
+  std::vector<int32_t> tshape_ip_checked_;
+  std::map<std::vector<int32_t>, bool> ip_checked_;
+
+  std::unordered_map<uint64_t, ListRef> flist_memo_;  // factor lists, global
+  std::unordered_map<uint64_t, ListRef> plist_memo_;  // product lists, per wave
+  std::unordered_map<uint64_t, int32_t> tlist_memo_;  // trace lists, per wave
+  std::vector<int32_t> list_shape_;                   // trace list -> trace shape (wave)
+  std::map<std::tuple<int, int, int>, int32_t> q0m_memo_, q1r_memo_;
+  std::map<std::tuple<int, int, int, int>, int32_t> q2m_memo_;
+
+  Wave w_;
+  int32_t wave_prod_slots_ = 0;
+  std::vector<std::pair<int32_t, ProdInst>> wave_prods_;  // (level, product)
+
+  int blk(int t) const { return t / block_size_; }
+
+  // DilutionScheme::operator[] and BlockIterator (include/dilution-iterator.hpp:
+  // 21-191, 306-356) for DilutionType::block.
+  std::vector<std::pair<int, int>> slice_pairs(int i, int nb) const {
+    int bsnk = 0, bsrc = 0;
+    for (int j = 0; j < i; ++j) {
+      ++bsnk;
+      if (bsnk == nb) {
+        ++bsrc;
+        bsnk = bsrc;
+      }
+    }
+    int const bs = block_size_;
+    std::vector<std::pair<int, int>> out;
+    for (int s = bsrc * bs; s < (bsrc + 1) * bs; ++s)
+      for (int k = bsnk * bs; k < (bsnk + 1) * bs; ++k) out.emplace_back(s, k);
+    if (bsrc != bsnk)
+      for (int s = bsnk * bs; s < (bsnk + 1) * bs; ++s)
+        for (int k = bsrc * bs; k < (bsrc + 1) * bs; ++k) out.emplace_back(s, k);
+    return out;
+  }
+
+  void begin_wave(int b) {
+    w_ = Wave{};
+    w_.block_pair = b;
+    wave_prod_slots_ = 0;
+    wave_prods_.clear();
+    plist_memo_.clear();
+    tlist_memo_.clear();
+    list_shape_.clear();
+  }
+
+  void end_wave() {
+    std::stable_sort(wave_prods_.begin(), wave_prods_.end(),
+                     [](auto const &x, auto const &y) { return x.first < y.first; });
+    int32_t level = -1;
+    for (size_t k = 0; k < wave_prods_.size(); ++k) {
+      while (level < wave_prods_[k].first) {
+        w_.prod_level_off.push_back(static_cast<int64_t>(k));
+        ++level;
+      }
+      w_.prods.push_back(wave_prods_[k].second);
+    }
+    w_.prod_level_off.push_back(static_cast<int64_t>(wave_prods_.size()));
+    w_.n_prod_slots = wave_prod_slots_;
+    double const e = s_.eds;
+    w_.flops_products = 8.0 * e * e * e * w_.prods.size();
+    double tr2 = 0, tr1 = 0;
+    for (auto const &l : w_.lists) {
+      double const n = static_cast<double>(s_.shapes[l.shape].i.size());
+      (l.b_base == INT32_MIN ? tr1 : tr2) += n;
+    }
+    w_.flops_traces = 8.0 * e * e * tr2 + 2.0 * e * tr1;
+    w_.n_trace_entries = static_cast<int64_t>(tr1 + tr2);
+    s_.waves.push_back(std::move(w_));
+  }
+
+  void finish() {
+    s_.n_factor_slots = n_factor_slots_;
+    auto fix = [&](int32_t slot) {
+      return slot >= 0 ? slot : n_factor_slots_ + (-slot - 1);
+    };
+    for (auto &w : s_.waves) {
+      for (auto &p : w.prods) {
+        p.a = fix(p.a);
+        p.b = fix(p.b);
+        p.c = fix(p.c);
+      }
+      for (auto &l : w.lists) {
+        l.a_base = fix(l.a_base);
+        if (l.b_base != INT32_MIN) l.b_base = fix(l.b_base);
+        else l.b_base = -1;
+      }
+      s_.max_prod_slots = std::max(s_.max_prod_slots, w.n_prod_slots);
+      s_.max_values = std::max(s_.max_values, w.n_values);
+      s_.max_terms = std::max<int64_t>(s_.max_terms, static_cast<int64_t>(w.terms.size()));
+      s_.max_lists = std::max<int64_t>(s_.max_lists, static_cast<int64_t>(w.lists.size()));
+      s_.flops_products += w.flops_products;
+      s_.flops_traces += w.flops_traces;
+      s_.n_terms += static_cast<int64_t>(w.terms.size());
+      s_.n_trace_entries += w.n_trace_entries;
+      s_.n_prods += static_cast<int64_t>(w.prods.size());
+    }
+    double const nev = dims_.nev, dilE = dims_.dilE;
+    s_.flops_factors = 8.0 * (s_.q0m.size() * 4.0 * nev * nev + s_.q0.size() * 4.0 * nev * dilE +
+                              s_.q1r.size() * 4.0 * nev * nev +
+                              s_.q1.size() * 16.0 * dilE * dilE * nev +
+                              s_.q2m.size() * 16.0 * dilE * nev * nev +
+                              s_.q2.size() * 64.0 * dilE * dilE * nev);
+  }
+
+  slaph_factor_index const &op(int type, int ql) const {
+    if (ql < 0 || ql >= plan_.n_factors[type])
+      throw ArgError("quark line index out of range in trace lookup");
+    return plan_.factors[type][ql];
+  }
+
+  int32_t vdv_code(slaph_factor_index const &o) const {
+    if (o.id_vdaggerv < 0 || o.id_vdaggerv >= plan_.n_vdv_ops)
+      throw ArgError("VdaggerV id out of range");
+    if (o.gamma < 0 || o.gamma > 15) throw ArgError("gamma index out of range");
+    return 2 * o.id_vdaggerv + (o.need_vdaggerv_daggering ? 1 : 0);
+  }
+
+  int32_t shape_id(std::vector<SymE> const &v) {
+    auto it = shape_ids_.find(v);
+    if (it != shape_ids_.end()) return it->second;
+    int32_t const id = static_cast<int32_t>(shapes_.size());
+    shapes_.push_back(v);
+    shape_ids_.emplace(v, id);
+    return id;
+  }
+
+  template <typename K, typename V>
+  int32_t intern(std::map<K, int32_t> &memo, K const &key, std::vector<V> &vec, V const &val) {
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    int32_t const id = static_cast<int32_t>(vec.size());
+    vec.push_back(val);
+    memo.emplace(key, id);
+    return id;
+  }
+
+  // DilutedFactorFactory<Q>::operator[](key).at(ql): one entry per rnd pair,
+  // in the order of the lookup table (src/DilutedFactorFactory.cpp:65,131,202).
+  ListRef factor_list(int type, int a, int b, int c, int ql) {
+    uint64_t const key = (static_cast<uint64_t>(type) << 62) |
+                         (static_cast<uint64_t>(a & 0x3FF) << 52) |
+                         (static_cast<uint64_t>(b & 0x3FF) << 42) |
+                         (static_cast<uint64_t>(c & 0x3FF) << 32) | static_cast<uint32_t>(ql);
+    auto it = flist_memo_.find(key);
+    if (it != flist_memo_.end()) return it->second;
+    auto const &o = op(type, ql);
+    int32_t const vdv = vdv_code(o);
+    int32_t const base = n_factor_slots_;
+    std::vector<SymE> entries;
+    for (int k = 0; k < o.n_rnd_pairs; ++k) {
+      int const r1 = o.rnd_pairs[2 * k], r2 = o.rnd_pairs[2 * k + 1];
+      if (r1 < 0 || r2 < 0 || r1 >= dims_.n_rnd || r2 >= dims_.n_rnd)
+        throw ArgError("random vector index out of range");
+      int32_t const slot = n_factor_slots_++;
+      if (type == 0) {  // key {t}
+        int32_t const m = intern(q0m_memo_, std::make_tuple(a, vdv, r2), s_.q0m, Q0MInst{a, vdv, r2});
+        s_.q0.push_back({a, m, r1, o.gamma, slot});
+      } else if (type == 1) {  // key {t, b}
+        int32_t const r = intern(q1r_memo_, std::make_tuple(a, vdv, r1), s_.q1r, Q1RInst{a, vdv, r1});
+        s_.q1.push_back({a, b, r, r2, o.gamma, slot});
+      } else {  // key {b1, t, b2}: a = t, b = b1, c = b2
+        int32_t const m =
+            intern(q2m_memo_, std::make_tuple(a, b, r1, vdv), s_.q2m, Q2MInst{a, b, r1, vdv});
+        s_.q2.push_back({a, c, m, r2, o.gamma, slot});
+      }
+      entries.push_back({r1, r2, 0});
+    }
+    uint64_t const skey = pack2(type, ql);
+    auto sit = fshape_memo_.find(skey);
+    int32_t shape;
+    if (sit == fshape_memo_.end()) {
+      shape = shape_id(entries);
+      fshape_memo_.emplace(skey, shape);
+    } else {
+      shape = sit->second;
+    }
+    ListRef ref{shape, base, 0};
+    flist_memo_.emplace(key, ref);
+    return ref;
+  }
+  ListRef q0(int t, int ql) { return factor_list(0, t, 0, 0, ql); }
+  ListRef q1(int t, int b, int ql) { return factor_list(1, t, b, 0, ql); }
+  ListRef q2(int b1, int t, int b2, int ql) { return factor_list(2, t, b1, b2, ql); }
+
+  // operator*(vector<DF>, vector<DF>), src/DilutedFactor.cpp:6-51.
+  ProdTemplate const &product_template(int32_t sl, int32_t sr) {
+    uint64_t const key = pack2(sl, sr);
+    auto it = ptemplate_memo_.find(key);
+    if (it != ptemplate_memo_.end()) return ptemplates_[it->second];
+    ProdTemplate t;
+    std::vector<SymE> out;
+    auto const &L = shapes_[sl];
+    auto const &R = shapes_[sr];
+    for (size_t x = 0; x < L.size(); ++x)
+      for (size_t y = 0; y < R.size(); ++y) {
+        if (!(L[x].r2 == R[y].r1 && L[x].r1 != R[y].r2)) continue;
+        if ((L[x].used & R[y].used) != 0u) continue;
+        t.pairs.emplace_back(static_cast<int32_t>(x), static_cast<int32_t>(y));
+        out.push_back({L[x].r1, R[y].r2,
+                       static_cast<uint16_t>(L[x].used | R[y].used | (1u << L[x].r2))});
+      }
+    if (out.empty()) throw EmptyError(kMulEmpty);
+    t.out_shape = shape_id(out);
+    int32_t const id = static_cast<int32_t>(ptemplates_.size());
+    ptemplates_.push_back(std::move(t));
+    ptemplate_memo_.emplace(key, id);
+    return ptemplates_[id];
+  }
+
+  // multiply<1,1> memo (include/DilutedFactor.hpp:164-187), per wave.
+  ListRef multiply(ListRef const &l, ListRef const &r) {
+    uint64_t const key = pack2(l.base, r.base);
+    auto it = plist_memo_.find(key);
+    if (it != plist_memo_.end()) return it->second;
+    ProdTemplate const &t = product_template(l.shape, r.shape);
+    int32_t const level = std::max(l.level, r.level) + 1;
+    int32_t const base = -(wave_prod_slots_ + 1);
+    for (auto const &pr : t.pairs) {
+      int32_t const slot = -(wave_prod_slots_ + 1);
+      ++wave_prod_slots_;
+      int32_t const a = l.base >= 0 ? l.base + pr.first : l.base - pr.first;
+      int32_t const b = r.base >= 0 ? r.base + pr.second : r.base - pr.second;
+      wave_prods_.push_back({level, ProdInst{a, b, slot}});
+    }
+    ListRef ref{t.out_shape, base, level};
+    plist_memo_.emplace(key, ref);
+    return ref;
+  }
+
+  // factor_to_trace(L, R) / factor_to_trace(F), src/DilutedTrace.cpp:84-165.
+  int32_t trace_shape(int32_t sl, int32_t sr) {
+    uint64_t const key = pack2(sl, sr);
+    auto it = tshape_memo_.find(key);
+    if (it != tshape_memo_.end()) return it->second;
+    TraceShape ts;
+    auto const &L = shapes_[sl];
+    if (sr >= 0) {
+      auto const &R = shapes_[sr];
+      for (size_t x = 0; x < L.size(); ++x)
+        for (size_t y = 0; y < R.size(); ++y) {
+          if (!(L[x].r2 == R[y].r1 && L[x].r1 == R[y].r2)) continue;
+          if ((L[x].used & R[y].used) != 0u) continue;
+          ts.i.push_back(static_cast<int32_t>(x));
+          ts.j.push_back(static_cast<int32_t>(y));
+          ts.mask.push_back(static_cast<uint16_t>(L[x].used | R[y].used | (1u << L[x].r2) |
+                                                  (1u << L[x].r1)));
+        }
+      if (ts.i.empty()) throw EmptyError(kTrEmpty2);
+    } else {
+      for (size_t x = 0; x < L.size(); ++x) {
+        if (L[x].r1 != L[x].r2) continue;
+        ts.i.push_back(static_cast<int32_t>(x));
+        ts.j.push_back(-1);
+        ts.mask.push_back(static_cast<uint16_t>(L[x].used | (1u << L[x].r1)));
+      }
+      if (ts.i.empty()) throw EmptyError(kTrEmpty1);
+    }
+    int32_t const id = static_cast<int32_t>(s_.shapes.size());
+    s_.shapes.push_back(std::move(ts));
+    tshape_memo_.emplace(key, id);
+    return id;
+  }
+
+  int32_t new_list(int32_t shape, ListRef const &a, ListRef const *b) {
+    TraceList tl;
+    tl.shape = shape;
+    tl.a_base = a.base;
+    tl.b_base = b ? b->base : INT32_MIN;
+    tl.val_off = w_.n_values;
+    w_.n_values += static_cast<int64_t>(s_.shapes[shape].i.size());
+    w_.lists.push_back(tl);
+    list_shape_.push_back(shape);
+    return static_cast<int32_t>(w_.lists.size()) - 1;
+  }
+  int32_t to_trace(ListRef const &l, ListRef const &r) {
+    return new_list(trace_shape(l.shape, r.shape), l, &r);
+  }
+  int32_t to_trace(ListRef const &f) { return new_list(trace_shape(f.shape, -1), f, nullptr); }
+
+  // DilutedTrace*Factory::build for one trace id, src/DilutedTraceFactory.cpp.
+  int32_t build_trace(int kind, int const *k, int const *c) {
+    switch (kind) {
+      case SLAPH_TR_Q1:
+        return to_trace(q1(k[0], blk(k[0]), c[0]));
+      case SLAPH_TR_Q1Q1:
+        return to_trace(q1(k[0], blk(k[1]), c[0]), q1(k[1], blk(k[0]), c[1]));
+      case SLAPH_TR_Q0Q2:
+        return to_trace(q0(k[1], c[1]), q2(blk(k[1]), k[0], blk(k[1]), c[0]));
+      case SLAPH_TR_Q1Q1Q1: {
+        ListRef const p = multiply(q1(k[0], blk(k[1]), c[0]), q1(k[1], blk(k[2]), c[1]));
+        return to_trace(p, q1(k[2], blk(k[0]), c[2]));
+      }
+      case SLAPH_TR_Q1Q0Q2: {
+        ListRef const p = multiply(q0(k[0], c[2]), q2(blk(k[0]), k[0], blk(k[1]), c[0]));
+        return to_trace(p, q1(k[1], blk(k[2]), c[1]));
+      }
+      case SLAPH_TR_Q1Q1Q1Q1: {
+        ListRef const p1 = multiply(q1(k[0], blk(k[1]), c[0]), q1(k[1], blk(k[2]), c[1]));
+        ListRef const p2 = multiply(q1(k[2], blk(k[3]), c[2]), q1(k[3], blk(k[0]), c[3]));
+        return to_trace(p1, p2);
+      }
+      case SLAPH_TR_Q2Q0Q2Q0: {
+        int const b0 = blk(k[0]), b2 = blk(k[2]);
+        ListRef const p1 = multiply(q0(k[0], c[0]), q2(b0, k[1], b2, c[1]));
+        ListRef const p2 = multiply(q0(k[2], c[2]), q2(b2, k[3], b0, c[3]));
+        return to_trace(p1, p2);
+      }
+      case SLAPH_TR_Q2Q0Q2Q0Q2Q0: {
+        int const b1 = blk(k[1]), b3 = blk(k[3]), b5 = blk(k[5]);
+        ListRef p = multiply(q2(b5, k[0], b1, c[1]), q0(k[1], c[2]));
+        p = multiply(p, q2(b1, k[2], b3, c[3]));
+        p = multiply(p, q0(k[3], c[4]));
+        p = multiply(p, q2(b3, k[4], b5, c[5]));
+        return to_trace(p, q0(k[5], c[0]));
+      }
+      default:
+        throw ArgError("unknown trace kind");
+    }
+  }
+
+  int32_t trace_list(slaph_trace_request const &r, int src, int snk) {
+    static int const arity[SLAPH_TR_KINDS] = {1, 2, 2, 3, 3, 4, 4, 6};
+    if (r.kind < 0 || r.kind >= SLAPH_TR_KINDS) throw ArgError("unknown trace kind");
+    if (r.tr_id < 0 || r.tr_id >= plan_.n_trace_ids[r.kind] || r.tr_id >= (1 << 24))
+      throw ArgError("trace id out of range");
+    if (r.n_loc != arity[r.kind]) throw ArgError("trace request location count mismatch");
+    // The reference memoises by the tuple of times (include/DilutedTraceFactory.hpp:
+    // 44-57); a pattern of source/sink locations gives that tuple from (src, snk).
+    int pattern = 0;
+    if (src != snk)
+      for (int l = 0; l < r.n_loc; ++l) pattern |= (r.loc[l] ? 1 : 0) << l;
+    uint64_t const key = (static_cast<uint64_t>(r.kind) << 61) |
+                         (static_cast<uint64_t>(r.tr_id) << 37) |
+                         (static_cast<uint64_t>(src & 0x3FF) << 27) |
+                         (static_cast<uint64_t>(snk & 0x3FF) << 17) |
+                         static_cast<uint64_t>(src == snk ? 0 : pattern);
+    auto it = tlist_memo_.find(key);
+    if (it != tlist_memo_.end()) return it->second;
+    int k[6];
+    for (int l = 0; l < r.n_loc; ++l) k[l] = r.loc[l] == 0 ? src : snk;
+    int const *c = plan_.trace_ql_ids[r.kind] + static_cast<int64_t>(r.tr_id) * arity[r.kind];
+    int32_t const id = build_trace(r.kind, k, c);
+    tlist_memo_.emplace(key, id);
+    return id;
+  }
+
+  // inner_product must have at least one summand (src/DilutedTrace.cpp:37-41,
+  // 75-79).  Masks depend only on the trace shapes, so the check is memoised.
+  void check_inner_product(Term const &t) {
+    std::vector<int32_t> key(t.n);
+    for (int k = 0; k < t.n; ++k) key[k] = list_shape_[t.list[k]];
+    if (ip_checked_.count(key)) return;
+    auto const &a = s_.shapes[key[0]].mask;
+    auto const &b = s_.shapes[key[1]].mask;
+    bool any = false;
+    if (t.n == 2) {
+      for (auto x : a)
+        for (auto y : b) any = any || (x & y) == 0;
+    } else {
+      auto const &c = s_.shapes[key[2]].mask;
+      for (auto x : a)
+        for (auto y : b)
+          for (auto z : c) any = any || (x & y & z) == 0;
+    }
+    if (!any) throw EmptyError(kIpEmpty);
+    ip_checked_.emplace(key, true);
+  }
+};
+
+}  // namespace
+
+Schedule build_schedule(slaph_dims const &dims, slaph_plan const &plan, int single_block_pair) {
+  if (dims.Lt < 1 || dims.dilT < 1 || dims.Lt % dims.dilT != 0 || dims.dilE < 1 || dims.nev < 1)
+    throw ArgError("invalid dims for the contraction schedule");
+  if (dims.Lt > 1024) throw UnsupportedError("Lt above 1024 is not supported");
+  if (dims.n_rnd > 16) throw UnsupportedError("at most 16 random vectors (16-bit used masks)");
+  Builder b(dims, plan);
+  return b.run(single_block_pair);
+}
+
+}  // namespace slaph

@@ -1,0 +1,111 @@
+// Launch wrappers of the engine's CUDA kernels (sm_103a).  All pointers are
+// device pointers; complex numbers are double2 (re, im); matrices are
+// column-major like Eigen::MatrixXcd.  Every wrapper enqueues on `stream` and
+// returns the cudaError_t of the launch.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace slaph {
+namespace dev {
+
+struct Q0MInst {
+  int32_t t, vdv, r2;
+};
+struct Q1RInst {
+  int32_t t, vdv, r1;
+};
+struct Q2MInst {
+  int32_t t, b1, r1, vdv;
+};
+struct Q0Inst {
+  int32_t t, m, r1, gamma, slot;
+};
+struct Q1Inst {
+  int32_t t, b, r, r2, gamma, slot;
+};
+struct Q2Inst {
+  int32_t t, b2, m, r2, gamma, slot;
+};
+struct ProdInst {
+  int32_t a, b, c;
+};
+struct TraceList {
+  int32_t shape;
+  int32_t a_base, b_base;
+  int64_t val_off;
+};
+struct Term {
+  int32_t n;
+  int32_t list[3];
+  int32_t out;
+  int32_t dt;
+};
+
+// Sizes every kernel needs.
+struct Geometry {
+  int32_t Lt, Lx, Ly, Lz, nev, dilE, n_rnd;
+  int32_t nb;       // number of time-dilution blocks (Lt / dilT)
+  int64_t dim_row;  // 3 * L^3
+};
+
+// Gamma table (src/Gamma.cpp:18-246) into constant memory.
+cudaError_t upload_gamma(cudaStream_t stream);
+
+// exp(-i p.x) for every op: phase[op][x] (create_momenta,
+// src/OperatorFactory.cpp:64-95).  mom: [n_ops][3].
+cudaError_t momenta(double2 *phase, int32_t const *mom, int32_t n_ops, Geometry g,
+                    cudaStream_t stream);
+
+// VdaggerV[vdv code 2*op][t] = V_t^H diag(phase[op] per site) V_t for every op
+// in ops[0..n) (src/OperatorFactory.cpp:292-300), FP64.  V: [Lt][nev][dim_row]
+// (each timeslice column-major).  vdv: [2*n_ops][Lt][nev][nev].
+cudaError_t vdaggerv_fp64(double2 *vdv, double2 const *V, double2 const *phase,
+                          int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
+                          cudaStream_t stream);
+// Identity blocks for code 2*op (and 2*op+1).
+cudaError_t vdaggerv_identity(double2 *vdv, int32_t op, Geometry g, cudaStream_t stream);
+// vdv[2*op+1][t] = vdv[2*op][t]^H for all ops, t.
+cudaError_t vdaggerv_daggers(double2 *vdv, int32_t n_ops, Geometry g, cudaStream_t stream);
+
+// Factor intermediates and factors (src/DilutedFactorFactory.cpp:34-253).
+cudaError_t q0m(double2 *out, Q0MInst const *inst, int64_t n, double2 const *vdv,
+                double2 const *noise, Geometry g, cudaStream_t stream);
+cudaError_t q1r(double2 *out, Q1RInst const *inst, int64_t n, double2 const *vdv,
+                double2 const *noise, Geometry g, cudaStream_t stream);
+cudaError_t q2m(double2 *out, Q2MInst const *inst, int64_t n, double2 const *vdv,
+                double2 const *peram, Geometry g, cudaStream_t stream);
+cudaError_t q0(double2 *slots, Q0Inst const *inst, int64_t n, double2 const *q0m,
+               double2 const *noise, Geometry g, cudaStream_t stream);
+cudaError_t q1(double2 *slots, Q1Inst const *inst, int64_t n, double2 const *q1r,
+               double2 const *peram, Geometry g, cudaStream_t stream);
+cudaError_t q2(double2 *slots, Q2Inst const *inst, int64_t n, double2 const *q2m,
+               double2 const *peram, Geometry g, cudaStream_t stream);
+
+// slots[c] = slots[a] * slots[b] (operator*, src/DilutedFactor.cpp:6-51).
+cudaError_t products(double2 *slots, ProdInst const *p, int64_t n, int32_t eds,
+                     cudaStream_t stream);
+
+// Trace values of every entry of every list (factor_to_trace,
+// src/DilutedTrace.cpp:84-165).  shape_i/shape_j: entry operand indices,
+// shape_off: [n_shapes+1] offsets into them.
+cudaError_t traces(double2 *values, TraceList const *lists, int64_t n_lists,
+                   int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
+                   double2 const *slots, int32_t eds, int64_t n_entries, cudaStream_t stream);
+
+// Term values (resolve_request / inner_product, src/Diagram.cpp:9-94,
+// src/DilutedTrace.cpp:5-82) with the native (0) or Kahan (1) accumulator.
+cudaError_t terms(double2 *term_val, Term const *t, int64_t n, TraceList const *lists,
+                  double2 const *values, uint16_t const *shape_mask,
+                  int64_t const *shape_off, int32_t kahan, cudaStream_t stream);
+
+// running[o] += term_val[idx[k]] for k in [seg[o], seg[o+1]) in order
+// (Diagram::assemble, src/Diagram.cpp:96-114).
+cudaError_t accumulate(double2 *running, int32_t const *seg_out, int64_t const *seg_off,
+                       int64_t n_seg, int32_t const *idx, double2 const *term_val,
+                       cudaStream_t stream);
+
+}  // namespace dev
+}  // namespace slaph

@@ -1,0 +1,140 @@
+"""Python mirror of the reference's hot-path classes over the C ABI.
+
+    OperatorFactory  ->  include/OperatorsForMesons.hpp:36-96
+    contract()       ->  include/Correlators.hpp:41-54
+    Diagram.write    ->  src/Diagram.cpp:132-147 + WriteHDF5Correlator
+
+All compute happens in libslaph_gb300.so on the current CUDA device; there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib as L
+
+FP64 = L.SLAPH_FP64
+MIXED = L.SLAPH_MIXED
+NATIVE = L.SLAPH_ACC_NATIVE
+KAHAN = L.SLAPH_ACC_KAHAN
+
+
+def _c128(a):
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    return a
+
+
+class Engine:
+    """One engine per lattice geometry (slaph_engine_*)."""
+
+    def __init__(self, dims: L.Dims):
+        self.dims = dims
+        h = C.c_void_p()
+        L.check(L.lib().slaph_engine_create(C.byref(dims), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().slaph_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_operators(self, plan):
+        L.check(L.lib().slaph_engine_set_operators(self._h, plan.vdv_ops, plan.n_vdv_ops,
+                                                   plan.index_of_unity))
+
+    def set_eigenvectors(self, t, V):
+        """V: timeslice t, complex (nev, 3L^3) C-order == (3L^3 x nev) column-major."""
+        V = _c128(V)
+        L.check(L.lib().slaph_engine_set_eigenvectors(self._h, t, L.dptr(V)))
+
+    def set_perambulator(self, r, P):
+        P = _c128(P)
+        L.check(L.lib().slaph_engine_set_perambulator(self._h, r, L.dptr(P)))
+
+    def set_random_vector(self, r, noise):
+        noise = _c128(noise)
+        L.check(L.lib().slaph_engine_set_random_vector(self._h, r, L.dptr(noise)))
+
+    def vdaggerv_build(self, precision=FP64):
+        L.check(L.lib().slaph_vdaggerv_build(self._h, precision))
+
+    def vdaggerv_fetch(self, op, t):
+        """nev x nev VdaggerV block as a numpy matrix M[i, j]."""
+        n = self.dims.nev
+        out = np.zeros(n * n, np.complex128)
+        L.check(L.lib().slaph_vdaggerv_fetch(self._h, op, t, L.dptr(out)))
+        return out.reshape(n, n).T.copy()
+
+    def contract(self, plan_ptr, precision=FP64, accumulator=NATIVE, single_block_pair=-1):
+        """[total_requests, Lt] complex correlators, divided by Lt."""
+        n = int(L.lib().slaph_plan_output_doubles(plan_ptr, self.dims.Lt))
+        out = np.zeros(max(n // 2, 1), np.complex128)
+        L.check(L.lib().slaph_contract(self._h, plan_ptr, precision, accumulator,
+                                       single_block_pair, L.dptr(out)))
+        return out[: n // 2].reshape(-1, self.dims.Lt)
+
+    def timings(self):
+        """ms: VdaggerV, factors, products+traces, assembly, planning; launches."""
+        out = np.zeros(6)
+        L.lib().slaph_engine_timings(self._h, L.dptr(out), 6)
+        return out
+
+    def stats(self):
+        out = np.zeros(6)
+        L.lib().slaph_engine_stats(self._h, L.dptr(out), 6)
+        return out
+
+
+class OperatorFactory:
+    """VdaggerV for every operator of the lookup table (OperatorFactory)."""
+
+    def __init__(self, engine: Engine, gd):
+        self.engine = engine
+        self.gd = gd
+        engine.set_operators(gd.plan)
+
+    def create_operators(self, precision=FP64):
+        self.engine.vdaggerv_build(precision)
+
+    def return_vdaggerv(self, index, t):
+        return self.engine.vdaggerv_fetch(index, t)
+
+
+def contract(engine: Engine, gd, precision=FP64, accumulator=NATIVE,
+             single_time_slice_combination=-1):
+    """Correlators of every diagram: {diagram: {dataset name: C[t]}}."""
+    flat = engine.contract(gd.plan_ptr, precision, accumulator, single_time_slice_combination)
+    out = {}
+    k = 0
+    for name, datasets in gd.output_layout():
+        out[name] = {}
+        for ds in datasets:
+            out[name][ds] = flat[k]
+            k += 1
+    return out
+
+
+def write_correlators(path, names, values):
+    """One reference-layout HDF5 file (WriteHDF5Correlator)."""
+    vals = np.ascontiguousarray(values, dtype=np.complex128)
+    n, lt = vals.shape
+    arr = (C.c_char_p * max(n, 1))(*[s.encode() for s in names])
+    L.check(L.lib().slaph_write_correlators_h5(str(path).encode(), n, arr, lt, L.dptr(vals)))
+
+
+def write_diagrams(output_path, correlators, filename_suffix):
+    """Diagram::write for every diagram: <output_path>/<diagram><suffix>."""
+    os.makedirs(output_path, exist_ok=True)
+    for name, ds in correlators.items():
+        names = list(ds)
+        write_correlators(os.path.join(output_path, name + filename_suffix), names,
+                          np.stack([ds[k] for k in names]))

@@ -96,6 +96,10 @@ def main(ref_root: Path):
             vals.append(v)
     np.savez_compressed(out / "goldens.npz", names=np.array(names), diagrams=np.array(diags),
                         values=np.stack(vals))
+    # Dilution-iterator golden text (tests/dilution-iterator/control.txt, the
+    # output of main/test-iterator.cpp), verbatim.
+    ctl = ref_root / "tests" / "dilution-iterator" / "control.txt"
+    (HERE / "dilution_control.txt").write_text(ctl.read_text())
     print(f"wrote {out}: {len(names)} golden datasets")
 
 
