@@ -1,0 +1,39 @@
+"""The C ABI library: loads without a GPU and exports every function that
+include/slaph_gb300.h declares (no compute calls)."""
+import re
+from pathlib import Path
+
+from conftest import REPO
+
+
+def declared_functions():
+    text = (REPO / "include" / "slaph_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*?\**\s*\**(slaph_[a-z0-9_]+)\s*\(",
+                       text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_engine_surface():
+    names = declared_functions()
+    for must in ("slaph_engine_create", "slaph_contract", "slaph_vdaggerv_build",
+                 "slaph_frontend_create", "slaph_write_correlators_h5", "slaph_last_error"):
+        assert must in names
+    assert len(names) >= 25
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    missing = [n for n in declared_functions() if not hasattr(engine_lib, n)]
+    assert not missing, missing
+
+
+def test_status_codes_and_messages_without_gpu(engine_lib):
+    import ctypes as C
+    from slaph_gb300 import _lib as L
+    h = C.c_void_p()
+    rc = engine_lib.slaph_frontend_create(b"/nonexistent/infile.in", 0, None, C.byref(h))
+    assert rc == L.SLAPH_ERR_PARSE
+    assert b"CANNOT open input file" in engine_lib.slaph_last_error()
+    assert engine_lib.slaph_trace_kind_arity(7) == 6
+    assert engine_lib.slaph_trace_kind_name(2) == b"trQ0Q2"
+    assert engine_lib.slaph_engine_create(None, C.byref(h)) == L.SLAPH_ERR_ARG
