@@ -245,6 +245,27 @@ int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt);
  * Returns the number of values written (<= n). */
 int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
 
+/* VdaggerV of one operator on one timeslice for callers that cannot let a
+ * library allocate device memory: hosts whose own allocator has reserved the
+ * device up front, and latency-critical loops that cannot afford the device
+ * synchronisation cudaMalloc/cudaFree may imply.  No counterpart in the
+ * reference (it has no GPU code); the result equals slaph_vdaggerv_fetch of
+ * slaph_vdaggerv_build(SLAPH_FP64).
+ *   V_t:  DEVICE pointer, 3*L^3 x nev complex, column-major (one timeslice)
+ *   out:  DEVICE pointer, nev x nev complex, column-major
+ *   momentum: host array of 3 ints; stream: a cudaStream_t (NULL = legacy)
+ * Allocates nothing: the phase table lives in a static device array of
+ * 4 MiB + 256 B, which every GPU that loads the library holds until the
+ * process exits, so L^3 may not exceed 262144 (64^3); larger lattices are
+ * rejected with SLAPH_ERR_ARG.  The first call on a device looks up that
+ * array's device address (once per device); make that first call before any
+ * stream capture.  The work is enqueued on `stream` and not waited for.
+ * Every call shares the one array: calls whose work overlaps on the GPU (other
+ * streams, or other host threads) race on it and must be serialised by the
+ * caller. */
+int slaph_vdaggerv_noalloc(const slaph_dims *dims, const double *V_t, const int32_t *momentum,
+                           double *out, void *stream);
+
 /* Device-resident statistics of the last contract: out[0] factors built,
  * out[1] products, out[2] traces, out[3] correlator terms, out[4] flops of
  * the factor stage, out[5] flops of products+traces. */
