@@ -46,6 +46,9 @@ void DevBuf::release() {
 
 namespace {
 
+// Upper bound of the split-precision VdaggerV scratch (timeslice batches).
+constexpr size_t kTcScratchCap = 24ULL << 30;
+
 template <typename T>
 void upload(DevBuf &b, std::vector<T> const &v, cudaStream_t s) {
   b.reserve(std::max<size_t>(1, v.size()) * sizeof(T));
@@ -156,19 +159,33 @@ void Engine::vdaggerv_build(int precision) {
   if (!ops_set_) throw StateError("slaph_engine_set_operators must be called first");
   if (precision != SLAPH_FP64 && precision != SLAPH_MIXED)
     throw ArgError("unknown precision mode");
-  if (precision == SLAPH_MIXED)
-    throw UnsupportedError("the split-precision VdaggerV path is not available in this build");
   launches_ = 0;
   std::vector<int32_t> computed;
   for (auto const &o : ops_)
     if (o.id != index_of_unity_) computed.push_back(o.id);
   DevBuf list;
   upload(list, computed, stream_);
+  int32_t const n_comp = static_cast<int32_t>(computed.size());
+  if (precision == SLAPH_MIXED) {
+    int sms = 0;
+    SLAPH_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+    int32_t const batch = dev::vdaggerv_tc_batch(geo_, std::max(n_comp, 1), sms, kTcScratchCap);
+    tc_scratch_.reserve(dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_comp, 1), batch));
+    err_.reserve(sizeof(int));
+    SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
+  }
   SLAPH_CK(cudaEventRecord(ev_[0], stream_));
-  launch(dev::vdaggerv_fp64(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
-                            list.as<int32_t>(), static_cast<int32_t>(computed.size()), 0,
-                            dims_.Lt, geo_, stream_),
-         "vdaggerv_fp64");
+  if (precision == SLAPH_MIXED) {
+    launch(dev::vdaggerv_tc(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
+                            list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_,
+                            tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_),
+           "vdaggerv_tc");
+    launches_ += 4LL * dims_.Lt - 1;
+  } else {
+    launch(dev::vdaggerv_fp64(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
+                              list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_, stream_),
+           "vdaggerv_fp64");
+  }
   if (index_of_unity_ >= 0)
     launch(dev::vdaggerv_identity(vdv_.as<double2>(), index_of_unity_, geo_, stream_),
            "vdaggerv_identity");
@@ -179,6 +196,13 @@ void Engine::vdaggerv_build(int precision) {
   SLAPH_CK(cudaEventSynchronize(ev_[1]));
   timings[0] = elapsed_ms(ev_[0], ev_[1]);
   timings[5] = static_cast<double>(launches_);
+  if (precision == SLAPH_MIXED) {
+    int code = 0;
+    SLAPH_CK(cudaMemcpy(&code, err_.as<void>(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (code != 0)
+      throw TimeoutError("split-precision VdaggerV: a bounded device wait gave up (stage " +
+                         std::to_string(code) + ")");
+  }
   vdv_built_ = true;
 }
 

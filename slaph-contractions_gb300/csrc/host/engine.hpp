@@ -76,7 +76,7 @@ class Engine {
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev_[8] = {};
 
-  DevBuf V_, peram_, noise_, phase_, vdv_, ops_dev_, mom_dev_;
+  DevBuf V_, peram_, noise_, phase_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
   std::vector<slaph_vdv_op> ops_;
   int32_t index_of_unity_ = -1;
   bool ops_set_ = false, vdv_built_ = false;

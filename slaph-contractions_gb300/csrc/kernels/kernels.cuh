@@ -65,6 +65,16 @@ cudaError_t momenta(double2 *phase, int32_t const *mom, int32_t n_ops, Geometry 
 cudaError_t vdaggerv_fp64(double2 *vdv, double2 const *V, double2 const *phase,
                           int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
                           cudaStream_t stream);
+// Split-BF16 tensor-core VdaggerV (vdv_tc.cu): same result as vdaggerv_fp64
+// to ~1e-13 relative.  scratch: device buffer of at least
+// vdaggerv_tc_scratch_bytes(g, n, batch) bytes, where batch timeslices are
+// processed per launch (vdaggerv_tc_batch picks it from the SM count and a
+// memory cap); err: device int, set non-zero when a bounded wait gave up.
+size_t vdaggerv_tc_scratch_bytes(Geometry g, int32_t n_ops, int32_t batch);
+int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes);
+cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, double2 const *phase,
+                        int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
+                        void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream);
 // Identity blocks for code 2*op (and 2*op+1).
 cudaError_t vdaggerv_identity(double2 *vdv, int32_t op, Geometry g, cudaStream_t stream);
 // vdv[2*op+1][t] = vdv[2*op][t]^H for all ops, t.

@@ -154,3 +154,99 @@ def test_vdaggerv_fp64_cfg2_full_volume(oracle_lib):
         for t in range(0, w.Lt, 7):
             m = eng.vdaggerv_fetch(op, t)
             assert np.sum(np.abs(m) ** 2) <= w.nev * (1 + 1e-10)
+
+
+# ---------------------------------------------------------------- mixed path
+# Split-BF16 tensor-core VdaggerV: 47-bit exact slices, exact FP32 chunk
+# accumulation, double-float promotion.  VdaggerV blocks within 1e-12 of the
+# FP64 path (relative to the block's largest entry); correlators within the
+# 1e-10 relative bound stated for the mixed path.
+REL_MIXED_VDV = 1e-12
+REL_MIXED_CORR = 1e-10
+
+
+@pytest.mark.parametrize("name", ["cfg1_4x8", "pipi_small"])
+def test_vdaggerv_mixed_matches_fp64_and_contract(name, oracle_lib):
+    from slaph_gb300 import synthetic
+    w = synthetic.CONFIGS[name] if name in synthetic.CONFIGS else synthetic.small_pipi()
+    gd, V, peram, noise = _synthetic_case(w)
+    eng = make_engine(gd, V, peram, noise)
+    eng.vdaggerv_build(0)
+    fp64 = {(op, t): eng.vdaggerv_fetch(op, t) for op in range(gd.plan.n_vdv_ops)
+            for t in range(gd.dims.Lt)}
+    eng.vdaggerv_build(1)
+    worst = 0.0
+    for (op, t), ref in fp64.items():
+        worst = max(worst, rel_err(eng.vdaggerv_fetch(op, t), ref))
+    print(f"{name}: mixed VdaggerV max rel err {worst:.2e}")
+    assert worst < REL_MIXED_VDV
+    vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
+    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+                          gd.output_doubles()).reshape(-1, gd.dims.Lt)
+    out = eng.contract(gd.plan_ptr, 1, 0)
+    e = rel_err(out, ref)
+    print(f"{name}: mixed correlators max rel err {e:.2e}")
+    assert e < REL_MIXED_CORR
+
+
+def test_mixed_l4_goldens(l4):
+    gd = l4["gd"]
+    eng = make_engine(gd, l4["V"], l4["peram"], l4["noise"])
+    eng.vdaggerv_build(1)
+    out = eng.contract(gd.plan_ptr, 1, 0)
+    names = [n for _, ds in gd.output_layout() for n in ds]
+    scale = max(np.max(np.abs(v)) for v in l4["golden"].values())
+    err = max(np.max(np.abs(v - l4["golden"][n])) for n, v in zip(names, out))
+    print(f"L4 mixed: max abs err {err:.2e} (scale {scale:.2e})")
+    assert err < REL_MIXED_CORR * scale
+
+
+def _vdv_columns_hp(V, phase, cols):
+    """VdaggerV columns V^H diag(phase per site) V[:, j] accumulated in
+    extended precision (np.longdouble: 80-bit on x86, IEEE quad on aarch64)."""
+    Vl = V.T.astype(np.clongdouble)                      # (dim_row, nev)
+    ph = np.repeat(phase.astype(np.clongdouble), 3)     # colour-expanded
+    out = {}
+    for j in cols:
+        w = ph * Vl[:, j]
+        out[j] = (np.conj(Vl) * w[:, None]).sum(axis=0)
+    return out
+
+
+def test_vdaggerv_mixed_cfg2_full_volume(oracle_lib):
+    """24^3 x 48, Nev 120, 13 computed momenta (K = 41472): both paths against
+    an extended-precision reference on sampled columns.  At this K the FP64
+    path's own rounding is ~1e-12 of the block's largest entry; the mixed path
+    must stay within 1e-12 as well."""
+    from slaph_gb300 import synthetic, GlobalData
+    from slaph_gb300.engine import Engine
+    w = synthetic.CONFIGS["cfg2_24x48_vdv"]
+    gd = GlobalData.from_infile(w.write_infile())
+    eng = Engine(gd.dims)
+    eng.set_operators(gd.plan)
+    V = {}
+    for t in range(w.Lt):
+        v = w.eigenvectors(t)
+        if t in (0, 31):
+            V[t] = v
+        eng.set_eigenvectors(t, v)
+    plan = gd.plan
+    ops = [o for o in range(plan.n_vdv_ops) if o != plan.index_of_unity][:3]
+    eng.vdaggerv_build(0)
+    fp64 = {(o, t): eng.vdaggerv_fetch(o, t) for o in ops for t in V}
+    eng.vdaggerv_build(1)
+    ms = eng.timings()[0]
+    mixed = {(o, t): eng.vdaggerv_fetch(o, t) for o in ops for t in V}
+    e_fp64 = e_mixed = 0.0
+    cols = [0, 37, 119]
+    for o in ops:
+        phase = oracle.momentum(w.L, w.L, w.L, tuple(plan.vdv_ops[o].momentum))
+        for t in V:
+            ref = _vdv_columns_hp(V[t], phase, cols)
+            scale = float(max(np.max(np.abs(r)) for r in ref.values()))
+            for j, r in ref.items():
+                e_fp64 = max(e_fp64, float(np.max(np.abs(fp64[o, t][:, j] - r))) / scale)
+                e_mixed = max(e_mixed, float(np.max(np.abs(mixed[o, t][:, j] - r))) / scale)
+    print(f"cfg2 VdaggerV vs extended precision: fp64 {e_fp64:.2e}, mixed {e_mixed:.2e}; "
+          f"mixed build {ms:.1f} ms")
+    assert e_mixed < REL_MIXED_VDV
