@@ -45,7 +45,9 @@ extern "C" {
 enum slaph_precision {
   SLAPH_FP64 = 0,  /* every product in FP64                                   */
   SLAPH_MIXED = 1  /* VdaggerV as split-BF16 tensor-core products with exact
-                      FP32 partial sums promoted to FP64; rest FP64            */
+                      FP32 partial sums; diluted traces as compensated
+                      double-float (2 x FP32) dot products; factors, products
+                      and the correlator sums in FP64                          */
 };
 
 enum slaph_accumulator {

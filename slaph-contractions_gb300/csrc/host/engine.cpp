@@ -180,7 +180,10 @@ void Engine::vdaggerv_build(int precision) {
                             list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_,
                             tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_),
            "vdaggerv_tc");
-    launches_ += 4LL * dims_.Lt - 1;
+    // three slicing kernels per timeslice, one GEMM per timeslice batch
+    int64_t const per = static_cast<int64_t>(
+        tc_scratch_.size() / dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_comp, 1), 1));
+    launches_ += 3LL * dims_.Lt + (dims_.Lt + per - 1) / std::max<int64_t>(per, 1) - 1;
   } else {
     launch(dev::vdaggerv_fp64(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
                               list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_, stream_),
@@ -300,7 +303,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   for (int32_t d = 0; d < plan->n_diagrams; ++d)
     if (plan->diagrams[d].n_requests > 0 && !plan->diagrams[d].requests)
       throw ArgError("diagram without request array");
-  launches_ = 0;
+  // launches_ continues the count of the preceding VdaggerV build: one gauge
+  // configuration = build + contract.
   auto const tp = std::chrono::steady_clock::now();
   prepare_schedule(plan, single_block_pair);
   double const plan_wall =
@@ -312,9 +316,11 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   int64_t const nev = dims_.nev;
 
   // ---- factors
+  bool const mixed = precision == SLAPH_MIXED;
   SLAPH_CK(cudaEventRecord(ev_[0], stream_));
-  slots_.reserve(sizeof(double2) * ms * std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots));
-  {
+  if (!mixed) {
+    slots_.reserve(sizeof(double2) * ms *
+                   std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots));
     DevBuf q0m, q1r, q2m;
     q0m.reserve(sizeof(double2) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
     q1r.reserve(sizeof(double2) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
@@ -340,6 +346,36 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
            "q2");
     SLAPH_CK(cudaEventRecord(ev_[1], stream_));
     SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
+  } else {
+    // Double-float matrices in both layouts: factors now, products per wave.
+    size_t const df_bytes =
+        sizeof(float4) * ms * std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots);
+    df_slots_.reserve(df_bytes);
+    df_slots_t_.reserve(df_bytes);
+    int64_t const n_vdv = 2LL * static_cast<int64_t>(ops_.size()) * dims_.Lt * nev * nev;
+    int64_t const n_noise = 4LL * nev * dims_.Lt * dims_.n_rnd;
+    int64_t const n_peram = peram_elems() * dims_.n_rnd;
+    DevBuf vdv_df, noise_df, peram_df, q0m, q1r, q2m;
+    vdv_df.reserve(sizeof(float4) * std::max<int64_t>(1, n_vdv));
+    noise_df.reserve(sizeof(float4) * n_noise);
+    peram_df.reserve(sizeof(float4) * n_peram);
+    launch(dev::to_df(vdv_df.as<float4>(), vdv_.as<double2>(), n_vdv, stream_), "to_df");
+    launch(dev::to_df(noise_df.as<float4>(), noise_.as<double2>(), n_noise, stream_), "to_df");
+    launch(dev::to_df(peram_df.as<float4>(), peram_.as<double2>(), n_peram, stream_), "to_df");
+    q0m.reserve(sizeof(float4) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
+    q1r.reserve(sizeof(float4) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
+    q2m.reserve(sizeof(float4) * std::max<int64_t>(1, s.q2m.size()) * eds * 4 * nev);
+    launch(dev::factors_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), q0m.as<float4>(),
+                           q1r.as<float4>(), q2m.as<float4>(), ds.q0m.as<dev::Q0MInst>(),
+                           s.q0m.size(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(),
+                           ds.q2m.as<dev::Q2MInst>(), s.q2m.size(), ds.q0.as<dev::Q0Inst>(),
+                           s.q0.size(), ds.q1.as<dev::Q1Inst>(), s.q1.size(),
+                           ds.q2.as<dev::Q2Inst>(), s.q2.size(), vdv_df.as<float4>(),
+                           noise_df.as<float4>(), peram_df.as<float4>(), geo_, stream_),
+           "factors_df");
+    launches_ += 5;
+    SLAPH_CK(cudaEventRecord(ev_[1], stream_));
+    SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
   }
   timings[1] = elapsed_ms(ev_[0], ev_[1]);
 
@@ -357,14 +393,30 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     auto const *prods = wb.prods.as<dev::ProdInst>();
     for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
       int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
-      if (e > b)
+      if (e <= b) continue;
+      if (mixed)
+        launch(dev::products_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), prods + b,
+                                e - b, eds, stream_),
+               "products_df");
+      else
         launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
     }
-    launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
-                       static_cast<int64_t>(w.lists.size()), ds.shape_i.as<int32_t>(),
-                       ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
-                       slots_.as<double2>(), eds, w.n_values, stream_),
-           "traces");
+    if (mixed) {
+      values_df_.reserve(sizeof(float4) * std::max<int64_t>(1, s.max_values));
+      launch(dev::traces_df(values_.as<double2>(), values_df_.as<float4>(), w.n_values,
+                            wb.lists.as<dev::TraceList>(), static_cast<int64_t>(w.lists.size()),
+                            ds.shape_i.as<int32_t>(), ds.shape_j.as<int32_t>(),
+                            ds.shape_off.as<int64_t>(), df_slots_.as<float4>(),
+                            df_slots_t_.as<float4>(), eds, stream_),
+             "traces_df");
+      ++launches_;
+    } else {
+      launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
+                         static_cast<int64_t>(w.lists.size()), ds.shape_i.as<int32_t>(),
+                         ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
+                         slots_.as<double2>(), eds, w.n_values, stream_),
+             "traces");
+    }
     SLAPH_CK(cudaEventRecord(ev_[3], stream_));
     launch(dev::terms(term_val_.as<double2>(), wb.terms.as<dev::Term>(),
                       static_cast<int64_t>(w.terms.size()), wb.lists.as<dev::TraceList>(),

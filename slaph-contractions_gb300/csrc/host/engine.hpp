@@ -83,7 +83,7 @@ class Engine {
   int64_t launches_ = 0;
 
   // Working buffers of the contraction.
-  DevBuf slots_, values_, term_val_, running_;
+  DevBuf slots_, df_slots_, df_slots_t_, values_, values_df_, term_val_, running_;
 
   std::unique_ptr<DeviceSchedule> sched_;
   slaph_plan const *sched_plan_ = nullptr;

@@ -105,6 +105,32 @@ cudaError_t traces(double2 *values, TraceList const *lists, int64_t n_lists,
                    int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
                    double2 const *slots, int32_t eds, int64_t n_entries, cudaStream_t stream);
 
+// Mixed path: matrices in double-float form (float4 = re hi, re lo, im hi,
+// im lo per complex), written as stored (dst_n) and transposed (dst_t); traces
+// as compensated FP32 dot products over unit-stride operands.
+cudaError_t split_df(float4 *dst_n, float4 *dst_t, double2 const *src, int64_t n, int32_t eds,
+                     cudaStream_t stream);
+// Mixed path: FP64 -> double-float (float4) copy.
+cudaError_t to_df(float4 *dst, double2 const *src, int64_t n, cudaStream_t stream);
+// Mixed path: all factor intermediates and factors in double-float; factors
+// written into the slot buffers in both layouts (sn stored, st transposed).
+cudaError_t factors_df(float4 *sn, float4 *st, float4 *q0m_buf, float4 *q1r_buf,
+                       float4 *q2m_buf, Q0MInst const *q0m_i, int64_t n_q0m,
+                       Q1RInst const *q1r_i, int64_t n_q1r, Q2MInst const *q2m_i, int64_t n_q2m,
+                       Q0Inst const *q0_i, int64_t n_q0, Q1Inst const *q1_i, int64_t n_q1,
+                       Q2Inst const *q2_i, int64_t n_q2, float4 const *vdv,
+                       float4 const *noise, float4 const *peram, Geometry g,
+                       cudaStream_t stream);
+// slots[c] = slots[a] * slots[b] in double-float, both layouts written.
+cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int64_t n,
+                        int32_t eds, cudaStream_t stream);
+// values_df: scratch of n_values float4 (double-float pairs), converted to
+// FP64 into values after the traces.
+cudaError_t traces_df(double2 *values, float4 *values_df, int64_t n_values,
+                      TraceList const *lists, int64_t n_lists, int32_t const *shape_i,
+                      int32_t const *shape_j, int64_t const *shape_off, float4 const *slots_n,
+                      float4 const *slots_t, int32_t eds, cudaStream_t stream);
+
 // Term values (resolve_request / inner_product, src/Diagram.cpp:9-94,
 // src/DilutedTrace.cpp:5-82) with the native (0) or Kahan (1) accumulator.
 cudaError_t terms(double2 *term_val, Term const *t, int64_t n, TraceList const *lists,

@@ -694,3 +694,483 @@ cudaError_t accumulate(double2 *running, int32_t const *seg_out, int64_t const *
 
 }  // namespace dev
 }  // namespace slaph
+
+// ---------------------------------------------------------------- double-float
+// Split-precision traces for the mixed path.  Matrices are converted once to
+// double-float form (hi = fl32(x), lo = fl32(x - hi)), 16 bytes per complex
+// like the FP64 layout; tr(L R) is then a compensated dot product on the FP32
+// units (error-free products via FMA, Knuth two-sum accumulation, the cross
+// terms hi*lo added to the compensation), summed in FP64 across the warp.
+// GB300's FP32 units are ~60x faster than its FP64 units.
+namespace slaph {
+namespace dev {
+namespace {
+
+// Each matrix in both layouts: dst_n[k] as stored (column-major), dst_t the
+// transpose, so that tr(L R) = sum_k L[k] R^T[k] reads both operands with
+// unit stride.
+__global__ void split_df_kernel(float4 *dst_n, float4 *dst_t, double2 const *src, int64_t n,
+                                int32_t eds) {
+  int64_t const k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  double2 const v = src[k];
+  float const rh = static_cast<float>(v.x), ih = static_cast<float>(v.y);
+  float const rl = static_cast<float>(v.x - static_cast<double>(rh));
+  float const il = static_cast<float>(v.y - static_cast<double>(ih));
+  float4 const f = make_float4(rh, rl, ih, il);
+  int64_t const ms = static_cast<int64_t>(eds) * eds;
+  int64_t const slot = k / ms;
+  int const e = static_cast<int>(k % ms);
+  int const i = e % eds, j = e / eds;
+  dst_n[k] = f;
+  dst_t[slot * ms + j + static_cast<int64_t>(eds) * i] = f;
+}
+
+struct DfAcc {
+  float s, c;
+};
+// acc += (xh + xl)(yh + yl), dropping xl*yl (relative 2^-48): error-free
+// product by FMA, Knuth two-sum into s, all low-order parts into c.
+__device__ __forceinline__ void df_mac(DfAcc &a, float xh, float xl, float yh, float yl) {
+  float const p = xh * yh;
+  float const e = fmaf(xh, yh, -p);
+  float const s = a.s + p;
+  float const bb = s - a.s;
+  float const err = (a.s - (s - bb)) + (p - bb);
+  a.s = s;
+  a.c += err + e + fmaf(xh, yl, xl * yh);
+}
+
+// Warp sum of (s, c) pairs with error-free two-sums (FP32 units only).
+__device__ __forceinline__ void df_warp_sum(DfAcc &a) {
+#pragma unroll
+  for (int sh = 16; sh > 0; sh >>= 1) {
+    float const os = __shfl_down_sync(0xffffffffu, a.s, sh);
+    float const oc = __shfl_down_sync(0xffffffffu, a.c, sh);
+    float const s = a.s + os;
+    float const bb = s - a.s;
+    float const err = (a.s - (s - bb)) + (os - bb);
+    a.s = s;
+    a.c += oc + err;
+  }
+}
+
+__global__ void __launch_bounds__(256) trace_df_kernel(float4 *values, TraceList const *lists,
+                                                       int32_t const *shape_i,
+                                                       int32_t const *shape_j,
+                                                       int64_t const *shape_off,
+                                                       float4 const *slots_n,
+                                                       float4 const *slots_t, int32_t eds) {
+  TraceList const L = lists[blockIdx.x];
+  int64_t const off = shape_off[L.shape];
+  int const n = static_cast<int>(shape_off[L.shape + 1] - off);
+  int const warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  int64_t const ms = static_cast<int64_t>(eds) * eds;
+  for (int e = warp; e < n; e += blockDim.x / 32) {
+    int const ia = shape_i[off + e], jb = shape_j[off + e];
+    float4 const *A = slots_n + (static_cast<int64_t>(L.a_base) + ia) * ms;
+    DfAcc ar{0.f, 0.f}, ai{0.f, 0.f};
+    if (jb >= 0) {
+      float4 const *B = slots_t + (static_cast<int64_t>(L.b_base) + jb) * ms;
+      DfAcc br{0.f, 0.f}, bi{0.f, 0.f};  // second accumulator set (ILP)
+      int64_t k = lane;
+      for (; k + 32 < ms; k += 64) {
+        float4 const x0 = A[k], y0 = B[k];
+        float4 const x1 = A[k + 32], y1 = B[k + 32];
+        df_mac(ar, x0.x, x0.y, y0.x, y0.y);
+        df_mac(br, x1.x, x1.y, y1.x, y1.y);
+        df_mac(ar, -x0.z, -x0.w, y0.z, y0.w);
+        df_mac(br, -x1.z, -x1.w, y1.z, y1.w);
+        df_mac(ai, x0.x, x0.y, y0.z, y0.w);
+        df_mac(bi, x1.x, x1.y, y1.z, y1.w);
+        df_mac(ai, x0.z, x0.w, y0.x, y0.y);
+        df_mac(bi, x1.z, x1.w, y1.x, y1.y);
+      }
+      for (; k < ms; k += 32) {
+        float4 const x = A[k], y = B[k];
+        df_mac(ar, x.x, x.y, y.x, y.y);
+        df_mac(ar, -x.z, -x.w, y.z, y.w);
+        df_mac(ai, x.x, x.y, y.z, y.w);
+        df_mac(ai, x.z, x.w, y.x, y.y);
+      }
+      df_mac(ar, br.s, br.c, 1.f, 0.f);
+      df_mac(ai, bi.s, bi.c, 1.f, 0.f);
+    } else {
+      for (int i = lane; i < eds; i += 32) {
+        float4 const x = A[i + static_cast<int64_t>(eds) * i];
+        df_mac(ar, x.x, x.y, 1.f, 0.f);
+        df_mac(ai, x.z, x.w, 1.f, 0.f);
+      }
+    }
+    df_warp_sum(ar);
+    df_warp_sum(ai);
+    if (lane == 0) values[L.val_off + e] = make_float4(ar.s, ar.c, ai.s, ai.c);
+  }
+}
+
+// Double-float (s, c) pairs to FP64: values[k] = (s_re + c_re, s_im + c_im).
+__global__ void df_to_fp64_kernel(double2 *dst, float4 const *src, int64_t n) {
+  int64_t const k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  float4 const v = src[k];
+  dst[k] = make_double2(static_cast<double>(v.x) + static_cast<double>(v.y),
+                        static_cast<double>(v.z) + static_cast<double>(v.w));
+}
+
+// Mixed path: C = A B in double-float arithmetic (operator*,
+// src/DilutedFactor.cpp:40-41).  Both operands are staged in shared memory as
+// stored (column-major): consecutive threads read consecutive rows of A and a
+// broadcast element of B.  The result is written in both layouts, so products
+// never pass through FP64.
+__global__ void __launch_bounds__(256) product_df_kernel(float4 *slots_n, float4 *slots_t,
+                                                         ProdInst const *p, int32_t eds) {
+  extern __shared__ float4 sdf[];
+  ProdInst const in = p[blockIdx.x];
+  int64_t const ms = static_cast<int64_t>(eds) * eds;
+  float4 *As = sdf, *Bs = sdf + ms;  // As[i + eds k] = A(i, k); Bs[k + eds j] = B(k, j)
+  float4 const *A = slots_n + in.a * ms;
+  float4 const *B = slots_n + in.b * ms;
+  for (int k = threadIdx.x; k < ms; k += blockDim.x) {
+    As[k] = A[k];
+    Bs[k] = B[k];
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < ms; k += blockDim.x) {
+    int const i = k % eds, j = k / eds;
+    DfAcc ar{0.f, 0.f}, ai{0.f, 0.f};
+    for (int q = 0; q < eds; ++q) {
+      float4 const x = As[i + eds * q];
+      float4 const y = Bs[q + eds * j];
+      df_mac(ar, x.x, x.y, y.x, y.y);
+      df_mac(ar, -x.z, -x.w, y.z, y.w);
+      df_mac(ai, x.x, x.y, y.z, y.w);
+      df_mac(ai, x.z, x.w, y.x, y.y);
+    }
+    float const rh = ar.s + ar.c, ih = ai.s + ai.c;
+    float4 const f = make_float4(rh, ar.c - (rh - ar.s), ih, ai.c - (ih - ai.s));
+    slots_n[in.c * ms + k] = f;
+    slots_t[in.c * ms + j + static_cast<int64_t>(eds) * i] = f;
+  }
+}
+
+}  // namespace
+
+cudaError_t split_df(float4 *dst_n, float4 *dst_t, double2 const *src, int64_t n, int32_t eds,
+                     cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  split_df_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(dst_n, dst_t, src,
+                                                                              n, eds);
+  return cudaGetLastError();
+}
+
+cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int64_t n,
+                        int32_t eds, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  size_t const smem = 2 * sizeof(float4) * eds * eds;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(product_df_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+  }
+  for (int64_t s0 = 0; s0 < n; s0 += 0x7fffffffLL) {
+    int64_t const c = n - s0 < 0x7fffffffLL ? n - s0 : 0x7fffffffLL;
+    product_df_kernel<<<static_cast<unsigned>(c), 256, smem, stream>>>(slots_n, slots_t, p + s0,
+                                                                        eds);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t traces_df(double2 *values, float4 *values_df, int64_t n_values,
+                      TraceList const *lists, int64_t n_lists, int32_t const *shape_i,
+                      int32_t const *shape_j, int64_t const *shape_off, float4 const *slots_n,
+                      float4 const *slots_t, int32_t eds, cudaStream_t stream) {
+  if (n_lists == 0) return cudaSuccess;
+  trace_df_kernel<<<static_cast<unsigned>(n_lists), 256, 0, stream>>>(
+      values_df, lists, shape_i, shape_j, shape_off, slots_n, slots_t, eds);
+  cudaError_t const e = cudaGetLastError();
+  if (e != cudaSuccess || n_values <= 0) return e;
+  df_to_fp64_kernel<<<static_cast<unsigned>((n_values + 255) / 256), 256, 0, stream>>>(
+      values, values_df, n_values);
+  return cudaGetLastError();
+}
+
+}  // namespace dev
+}  // namespace slaph
+
+// ---------------------------------------------------------------- df factors
+// Mixed path: the diluted-factor kernels above in double-float arithmetic.
+// Inputs (VdaggerV, perambulators, noise) are converted once per
+// configuration; the factors are written in both layouts for the products and
+// traces.  Same formulas and reference lines as the FP64 kernels.
+namespace slaph {
+namespace dev {
+namespace {
+
+struct CDf {
+  DfAcc r, i;
+};
+__device__ __forceinline__ CDf cdf_zero() { return CDf{{0.f, 0.f}, {0.f, 0.f}}; }
+// acc += x * y
+__device__ __forceinline__ void cdf_mac(CDf &a, float4 x, float4 y) {
+  df_mac(a.r, x.x, x.y, y.x, y.y);
+  df_mac(a.r, -x.z, -x.w, y.z, y.w);
+  df_mac(a.i, x.x, x.y, y.z, y.w);
+  df_mac(a.i, x.z, x.w, y.x, y.y);
+}
+// acc += conj(x) * y
+__device__ __forceinline__ void cdf_macc(CDf &a, float4 x, float4 y) {
+  df_mac(a.r, x.x, x.y, y.x, y.y);
+  df_mac(a.r, x.z, x.w, y.z, y.w);
+  df_mac(a.i, x.x, x.y, y.z, y.w);
+  df_mac(a.i, -x.z, -x.w, y.x, y.y);
+}
+__device__ __forceinline__ float4 cdf_value(CDf const &a) {
+  float const rh = a.r.s + a.r.c, ih = a.i.s + a.i.c;
+  return make_float4(rh, a.r.c - (rh - a.r.s), ih, a.i.c - (ih - a.i.s));
+}
+// exact for the gamma values +-1, +-i
+__device__ __forceinline__ float4 gamma_mul(double2 g, float4 v) {
+  if (g.y == 0.0) return g.x > 0 ? v : make_float4(-v.x, -v.y, -v.z, -v.w);
+  return g.y > 0 ? make_float4(-v.z, -v.w, v.x, v.y) : make_float4(v.z, v.w, -v.x, -v.y);
+}
+__device__ __forceinline__ float4 conj_df(float4 v) { return make_float4(v.x, v.y, -v.z, -v.w); }
+
+__global__ void to_df_kernel(float4 *dst, double2 const *src, int64_t n) {
+  int64_t const k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  double2 const v = src[k];
+  float const rh = static_cast<float>(v.x), ih = static_cast<float>(v.y);
+  dst[k] = make_float4(rh, static_cast<float>(v.x - static_cast<double>(rh)), ih,
+                       static_cast<float>(v.y - static_cast<double>(ih)));
+}
+
+__device__ __forceinline__ float4 const *vdv_block_df(float4 const *vdv, int code, int t,
+                                                      Geometry const &g) {
+  return vdv + (static_cast<int64_t>(code) * g.Lt + t) * g.nev * static_cast<int64_t>(g.nev);
+}
+
+__global__ void q0m_df_kernel(float4 *out, Q0MInst const *inst, float4 const *vdv,
+                              float4 const *noise, Geometry g) {
+  Q0MInst const in = inst[blockIdx.y];
+  int const nev = g.nev, eds = 4 * g.dilE;
+  int const k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nev * eds) return;
+  int const v = k % nev, c = k / nev;
+  int const e = c % g.dilE, d = c / g.dilE;
+  float4 const *m = vdv_block_df(vdv, in.vdv, in.t, g);
+  float4 const *rho = noise + static_cast<int64_t>(in.r2) * g.Lt * 4 * nev;
+  CDf acc = cdf_zero();
+  for (int w = e; w < nev; w += g.dilE)
+    cdf_mac(acc, rho[d + 4 * (w + static_cast<int64_t>(nev) * in.t)],
+            m[v + static_cast<int64_t>(nev) * w]);
+  out[static_cast<int64_t>(blockIdx.y) * nev * eds + k] = cdf_value(acc);
+}
+
+__global__ void q1r_df_kernel(float4 *out, Q1RInst const *inst, float4 const *vdv,
+                              float4 const *noise, Geometry g) {
+  Q1RInst const in = inst[blockIdx.y];
+  int const nev = g.nev, eds = 4 * g.dilE;
+  int const k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nev * eds) return;
+  int const a = k % eds, j = k / eds;
+  int const e = a % g.dilE, d = a / g.dilE;
+  float4 const *m = vdv_block_df(vdv, in.vdv, in.t, g);
+  float4 const *rho = noise + static_cast<int64_t>(in.r1) * g.Lt * 4 * nev;
+  CDf acc = cdf_zero();
+  for (int v = e; v < nev; v += g.dilE)
+    cdf_macc(acc, rho[d + 4 * (v + static_cast<int64_t>(nev) * in.t)],
+             m[v + static_cast<int64_t>(nev) * j]);
+  out[static_cast<int64_t>(blockIdx.y) * nev * eds + k] = cdf_value(acc);
+}
+
+__global__ void __launch_bounds__(256) q2m_df_kernel(float4 *out, Q2MInst const *inst,
+                                                     float4 const *vdv, float4 const *peram,
+                                                     Geometry g) {
+  __shared__ float4 As[KT][MT + 1];
+  __shared__ float4 Bs[KT][NT];
+  Q2MInst const in = inst[blockIdx.z];
+  int const nev = g.nev, eds = 4 * g.dilE;
+  int const ntile = (nev + NT - 1) / NT, mtile = (eds + MT - 1) / MT;
+  int const row = blockIdx.y;
+  int const v0 = (blockIdx.x % ntile) * NT;
+  int const a0 = (blockIdx.x / ntile) * MT;
+  if (a0 >= mtile * MT) return;
+  int const tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  int64_t const rows = peram_rows(g);
+  float4 const *P = peram + static_cast<int64_t>(in.r1) * rows * g.nb * 4 * g.dilE +
+                    (static_cast<int64_t>(4 * in.t + row) * nev) +
+                    rows * (static_cast<int64_t>(in.b1) * eds);
+  float4 const *m = vdv_block_df(vdv, in.vdv, in.t, g);
+  CDf acc[2][4];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = cdf_zero();
+  float4 const z = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int w0 = 0; w0 < nev; w0 += KT) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      int const k = tid + 256 * q;
+      int const ww = k % KT, aa = k / KT;
+      int const w = w0 + ww, a = a0 + aa;
+      As[ww][aa] = (w < nev && a < eds) ? P[w + rows * a] : z;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int const k = tid + 256 * q;
+      int const ww = k % KT, vv = k / KT;
+      int const w = w0 + ww, v = v0 + vv;
+      Bs[ww][vv] = (w < nev && v < nev) ? m[w + static_cast<int64_t>(nev) * v] : z;
+    }
+    __syncthreads();
+    for (int kk = 0; kk < KT; ++kk) {
+      float4 a[2], b[4];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) a[p] = As[kk][ty + 16 * p];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) b[q] = Bs[kk][tx + 16 * q];
+#pragma unroll
+      for (int p = 0; p < 2; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cdf_macc(acc[p][q], a[p], b[q]);
+    }
+    __syncthreads();
+  }
+  float4 *o = out + static_cast<int64_t>(blockIdx.z) * eds * 4 * nev;
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int const a = a0 + ty + 16 * p, v = v0 + tx + 16 * q;
+      if (a < eds && v < nev)
+        o[a + static_cast<int64_t>(eds) * (row * nev + v)] = cdf_value(acc[p][q]);
+    }
+}
+
+__device__ __forceinline__ void store_factor_df(float4 *sn, float4 *st, int slot, int k, int eds,
+                                                float4 v) {
+  int64_t const ms = static_cast<int64_t>(eds) * eds;
+  int const i = k % eds, j = k / eds;
+  sn[slot * ms + k] = v;
+  st[slot * ms + j + static_cast<int64_t>(eds) * i] = v;
+}
+
+__global__ void q0_df_kernel(float4 *sn, float4 *st, Q0Inst const *inst, float4 const *q0m,
+                             float4 const *noise, Geometry g) {
+  Q0Inst const in = inst[blockIdx.y];
+  int const nev = g.nev, dilE = g.dilE, eds = 4 * dilE;
+  int const k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= eds * eds) return;
+  int const a = k % eds, b = k / eds;
+  int const d = b / dilE;
+  int const gr = c_gamma_row[in.gamma][d];
+  CDf acc = cdf_zero();
+  if (a / dilE == gr) {
+    int const e1 = a % dilE;
+    float4 const *M = q0m + static_cast<int64_t>(in.m) * nev * eds;
+    float4 const *rho = noise + static_cast<int64_t>(in.r1) * g.Lt * 4 * nev;
+    double2 const val = c_gamma_val[in.gamma][d];
+    for (int v = e1; v < nev; v += dilE)
+      cdf_mac(acc, gamma_mul(val, M[v + static_cast<int64_t>(nev) * b]),
+              conj_df(rho[gr + 4 * (v + static_cast<int64_t>(nev) * in.t)]));
+  }
+  store_factor_df(sn, st, in.slot, k, eds, cdf_value(acc));
+}
+
+__global__ void q1_df_kernel(float4 *sn, float4 *st, Q1Inst const *inst, float4 const *q1r,
+                             float4 const *peram, Geometry g) {
+  Q1Inst const in = inst[blockIdx.y];
+  int const nev = g.nev, dilE = g.dilE, eds = 4 * dilE;
+  int const k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= eds * eds) return;
+  int const a = k % eds, c = k / eds;
+  int const row = a / dilE;
+  int64_t const rows = peram_rows(g);
+  float4 const *R = q1r + static_cast<int64_t>(in.r) * nev * eds;
+  float4 const *P = peram + static_cast<int64_t>(in.r2) * rows * g.nb * 4 * g.dilE +
+                    static_cast<int64_t>(4 * in.t + c_gamma_row[in.gamma][row]) * nev +
+                    rows * (static_cast<int64_t>(in.b) * eds + c);
+  CDf acc = cdf_zero();
+  for (int v = 0; v < nev; ++v) cdf_mac(acc, R[a + static_cast<int64_t>(eds) * v], P[v]);
+  store_factor_df(sn, st, in.slot, k, eds, gamma_mul(c_gamma_val[in.gamma][row], cdf_value(acc)));
+}
+
+__global__ void q2_df_kernel(float4 *sn, float4 *st, Q2Inst const *inst, float4 const *q2m,
+                             float4 const *peram, Geometry g) {
+  Q2Inst const in = inst[blockIdx.y];
+  int const nev = g.nev, dilE = g.dilE, eds = 4 * dilE;
+  int const k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= eds * eds) return;
+  int const a = k % eds, c = k / eds;
+  int const r = a / dilE;
+  int64_t const rows = peram_rows(g);
+  float4 const *M = q2m + static_cast<int64_t>(in.m) * eds * 4 * nev;
+  float4 const *Pr = peram + static_cast<int64_t>(in.r2) * rows * g.nb * 4 * g.dilE +
+                     rows * (static_cast<int64_t>(in.b2) * eds + c);
+  CDf total = cdf_zero();
+  for (int bd = 0; bd < 4; ++bd) {
+    float4 const *P = Pr + static_cast<int64_t>(4 * in.t + c_gamma_row[in.gamma][bd]) * nev;
+    float4 const *Mb = M + a + static_cast<int64_t>(eds) * bd * nev;
+    bool const flip = (bd + r == 3) || (bd - r > 1) || (r - bd > 1);
+    double2 const val = c_gamma_val[in.gamma][bd];
+    double2 const s = flip ? make_double2(-val.x, -val.y) : val;
+    for (int v = 0; v < nev; ++v)
+      cdf_mac(total, gamma_mul(s, Mb[static_cast<int64_t>(eds) * v]), P[v]);
+  }
+  store_factor_df(sn, st, in.slot, k, eds, cdf_value(total));
+}
+
+int blocks256(int64_t n) { return static_cast<int>((n + 255) / 256); }
+
+}  // namespace
+
+cudaError_t to_df(float4 *dst, double2 const *src, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  to_df_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(dst, src, n);
+  return cudaGetLastError();
+}
+
+cudaError_t factors_df(float4 *sn, float4 *st, float4 *q0m_buf, float4 *q1r_buf,
+                       float4 *q2m_buf, Q0MInst const *q0m_i, int64_t n_q0m,
+                       Q1RInst const *q1r_i, int64_t n_q1r, Q2MInst const *q2m_i, int64_t n_q2m,
+                       Q0Inst const *q0_i, int64_t n_q0, Q1Inst const *q1_i, int64_t n_q1,
+                       Q2Inst const *q2_i, int64_t n_q2, float4 const *vdv,
+                       float4 const *noise, float4 const *peram, Geometry g,
+                       cudaStream_t stream) {
+  int const eds = 4 * g.dilE;
+  int64_t const per_m = static_cast<int64_t>(g.nev) * eds;
+  int64_t const per_f = static_cast<int64_t>(eds) * eds;
+  cudaError_t e;
+  e = chunked(q0m_i, n_q0m, [&](Q0MInst const *p, int c, int64_t s) {
+    q0m_df_kernel<<<dim3(blocks256(per_m), c), 256, 0, stream>>>(q0m_buf + s * per_m, p, vdv,
+                                                                 noise, g);
+  });
+  if (e != cudaSuccess) return e;
+  e = chunked(q1r_i, n_q1r, [&](Q1RInst const *p, int c, int64_t s) {
+    q1r_df_kernel<<<dim3(blocks256(per_m), c), 256, 0, stream>>>(q1r_buf + s * per_m, p, vdv,
+                                                                 noise, g);
+  });
+  if (e != cudaSuccess) return e;
+  int const ntile = (g.nev + NT - 1) / NT, mtile = (eds + MT - 1) / MT;
+  int64_t const per_q2m = static_cast<int64_t>(eds) * 4 * g.nev;
+  e = chunked(q2m_i, n_q2m, [&](Q2MInst const *p, int c, int64_t s) {
+    q2m_df_kernel<<<dim3(ntile * mtile, 4, c), 256, 0, stream>>>(q2m_buf + s * per_q2m, p, vdv,
+                                                                 peram, g);
+  });
+  if (e != cudaSuccess) return e;
+  e = chunked(q0_i, n_q0, [&](Q0Inst const *p, int c, int64_t) {
+    q0_df_kernel<<<dim3(blocks256(per_f), c), 256, 0, stream>>>(sn, st, p, q0m_buf, noise, g);
+  });
+  if (e != cudaSuccess) return e;
+  e = chunked(q1_i, n_q1, [&](Q1Inst const *p, int c, int64_t) {
+    q1_df_kernel<<<dim3(blocks256(per_f), c), 256, 0, stream>>>(sn, st, p, q1r_buf, peram, g);
+  });
+  if (e != cudaSuccess) return e;
+  return chunked(q2_i, n_q2, [&](Q2Inst const *p, int c, int64_t) {
+    q2_df_kernel<<<dim3(blocks256(per_f), c), 256, 0, stream>>>(sn, st, p, q2m_buf, peram, g);
+  });
+}
+
+}  // namespace dev
+}  // namespace slaph

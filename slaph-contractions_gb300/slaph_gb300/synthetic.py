@@ -154,3 +154,16 @@ def small_pipi(L=4, Lt=8, nev=16, n_rnd=5, dilT=4, dilE=4, seed=404):
                      "C4cB:Q0:Op2:Q0:Op2:Q0:Op2:Q0:Op2:P0,1",
                      "C4cV:Q0:Op2:Q0:Op2:Q0:Op2:Q0:Op2:P0,1"],
         seed=seed, description="pipi diagram set on a small lattice")
+
+
+# Small case of the 32^3x64 diagram set for kernel profiles: 16^3 x 32, Nev 64,
+# momenta |p|^2 <= 1.  Eigenvectors (400 MB) exceed L2; a few GB on the device.
+CONFIGS["prof_16x32_pipi"] = Workload(
+    "prof_16x32_pipi", Lt=32, L=16, nev=64, n_rnd=5, dilT=16, dilE=8,
+    operators=[o.replace("p0,1,2,3,4", "p0,1") for o in PION_RHO_OPERATORS],
+    correlators=(["C2c:Q0:Op9:Q0:Op9:P0,1"]
+                 + [f"C3c:Q0:Op9:Q0:Op{k}:Q0:Op9:P0,1" for k in range(9)]
+                 + ["C4cD:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1",
+                    "C4cB:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1",
+                    "C4cV:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1"]),
+    seed=505, orthonormal=False, description="profiling case: 16^3x32 Nev=64 pipi")
