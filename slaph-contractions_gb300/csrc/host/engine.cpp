@@ -385,7 +385,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   int64_t const n_run = std::max<int64_t>(1, s.n_outputs * dims_.Lt);
   running_.reserve(sizeof(double2) * n_run);
   SLAPH_CK(cudaMemsetAsync(running_.as<void>(), 0, sizeof(double2) * n_run, stream_));
-  double t_pt = 0, t_as = 0;
+  double t_pt = 0, t_as = 0, t_tr = 0;
+  int64_t n_tr = 0;
   for (size_t wi = 0; wi < s.waves.size(); ++wi) {
     Wave const &w = s.waves[wi];
     auto &wb = *ds.waves[wi];
@@ -401,22 +402,27 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
       else
         launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
     }
+    SLAPH_CK(cudaEventRecord(ev_[5], stream_));
     if (mixed) {
       values_df_.reserve(sizeof(float4) * std::max<int64_t>(1, s.max_values));
-      launch(dev::traces_df(values_.as<double2>(), values_df_.as<float4>(), w.n_values,
-                            wb.lists.as<dev::TraceList>(), static_cast<int64_t>(w.lists.size()),
-                            ds.shape_i.as<int32_t>(), ds.shape_j.as<int32_t>(),
-                            ds.shape_off.as<int64_t>(), df_slots_.as<float4>(),
-                            df_slots_t_.as<float4>(), eds, stream_),
+      launch(dev::traces_df(values_df_.as<float4>(), wb.lists.as<dev::TraceList>(),
+                            static_cast<int64_t>(w.lists.size()), ds.shape_i.as<int32_t>(),
+                            ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
+                            df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds, stream_),
              "traces_df");
-      ++launches_;
+      SLAPH_CK(cudaEventRecord(ev_[6], stream_));
+      launch(dev::df_values_to_fp64(values_.as<double2>(), values_df_.as<float4>(), w.n_values,
+                                    stream_),
+             "df_values_to_fp64");
     } else {
       launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
                          static_cast<int64_t>(w.lists.size()), ds.shape_i.as<int32_t>(),
                          ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
                          slots_.as<double2>(), eds, w.n_values, stream_),
              "traces");
+      SLAPH_CK(cudaEventRecord(ev_[6], stream_));
     }
+    bool const traced = !w.lists.empty();
     SLAPH_CK(cudaEventRecord(ev_[3], stream_));
     launch(dev::terms(term_val_.as<double2>(), wb.terms.as<dev::Term>(),
                       static_cast<int64_t>(w.terms.size()), wb.lists.as<dev::TraceList>(),
@@ -432,11 +438,17 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     SLAPH_CK(cudaEventSynchronize(ev_[4]));
     t_pt += elapsed_ms(ev_[2], ev_[3]);
     t_as += elapsed_ms(ev_[3], ev_[4]);
+    if (traced) {
+      t_tr += elapsed_ms(ev_[5], ev_[6]);
+      ++n_tr;
+    }
   }
   timings[2] = t_pt;
   timings[3] = t_as;
   timings[4] = plan_wall * 1e3;
   timings[5] = static_cast<double>(launches_);
+  timings[6] = t_tr;
+  timings[7] = static_cast<double>(n_tr);
 
   // ---- output: C[t] = correlator[t][i] / Lt (src/Diagram.cpp:141-143)
   std::vector<double2> host(static_cast<size_t>(s.n_outputs * dims_.Lt));

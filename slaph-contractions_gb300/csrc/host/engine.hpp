@@ -66,7 +66,7 @@ class Engine {
   void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
                 double *corr_out);
 
-  double timings[6] = {0, 0, 0, 0, 0, 0};
+  double timings[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   double stats[6] = {0, 0, 0, 0, 0, 0};
 
  private:

@@ -124,12 +124,15 @@ cudaError_t factors_df(float4 *sn, float4 *st, float4 *q0m_buf, float4 *q1r_buf,
 // slots[c] = slots[a] * slots[b] in double-float, both layouts written.
 cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int64_t n,
                         int32_t eds, cudaStream_t stream);
-// values_df: scratch of n_values float4 (double-float pairs), converted to
-// FP64 into values after the traces.
-cudaError_t traces_df(double2 *values, float4 *values_df, int64_t n_values,
-                      TraceList const *lists, int64_t n_lists, int32_t const *shape_i,
-                      int32_t const *shape_j, int64_t const *shape_off, float4 const *slots_n,
-                      float4 const *slots_t, int32_t eds, cudaStream_t stream);
+// Trace values as double-float pairs (re_hi, re_lo, im_hi, im_lo) into
+// values_df, one entry per (list, shape entry).
+cudaError_t traces_df(float4 *values_df, TraceList const *lists, int64_t n_lists,
+                      int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
+                      float4 const *slots_n, float4 const *slots_t, int32_t eds,
+                      cudaStream_t stream);
+// values[i] = hi + lo of values_df[i], the FP64 trace values the terms read.
+cudaError_t df_values_to_fp64(double2 *values, float4 const *values_df, int64_t n_values,
+                              cudaStream_t stream);
 
 // Term values (resolve_request / inner_product, src/Diagram.cpp:9-94,
 // src/DilutedTrace.cpp:5-82) with the native (0) or Kahan (1) accumulator.

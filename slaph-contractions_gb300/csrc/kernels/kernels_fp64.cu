@@ -881,15 +881,19 @@ cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int
   return cudaGetLastError();
 }
 
-cudaError_t traces_df(double2 *values, float4 *values_df, int64_t n_values,
-                      TraceList const *lists, int64_t n_lists, int32_t const *shape_i,
-                      int32_t const *shape_j, int64_t const *shape_off, float4 const *slots_n,
-                      float4 const *slots_t, int32_t eds, cudaStream_t stream) {
+cudaError_t traces_df(float4 *values_df, TraceList const *lists, int64_t n_lists,
+                      int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
+                      float4 const *slots_n, float4 const *slots_t, int32_t eds,
+                      cudaStream_t stream) {
   if (n_lists == 0) return cudaSuccess;
   trace_df_kernel<<<static_cast<unsigned>(n_lists), 256, 0, stream>>>(
       values_df, lists, shape_i, shape_j, shape_off, slots_n, slots_t, eds);
-  cudaError_t const e = cudaGetLastError();
-  if (e != cudaSuccess || n_values <= 0) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t df_values_to_fp64(double2 *values, float4 const *values_df, int64_t n_values,
+                              cudaStream_t stream) {
+  if (n_values <= 0) return cudaSuccess;
   df_to_fp64_kernel<<<static_cast<unsigned>((n_values + 255) / 256), 256, 0, stream>>>(
       values, values_df, n_values);
   return cudaGetLastError();

@@ -64,6 +64,16 @@ class Engine:
         noise = _c128(noise)
         L.check(L.lib().slaph_engine_set_random_vector(self._h, r, L.dptr(noise)))
 
+    @staticmethod
+    def pin(arr):
+        """Page-lock a C-contiguous numpy array (slaph_host_register)."""
+        assert arr.flags["C_CONTIGUOUS"]
+        L.check(L.lib().slaph_host_register(arr.ctypes.data, arr.nbytes))
+
+    @staticmethod
+    def unpin(arr):
+        L.check(L.lib().slaph_host_unregister(arr.ctypes.data))
+
     def vdaggerv_build(self, precision=FP64):
         L.check(L.lib().slaph_vdaggerv_build(self._h, precision))
 
@@ -83,9 +93,10 @@ class Engine:
         return out[: n // 2].reshape(-1, self.dims.Lt)
 
     def timings(self):
-        """ms: VdaggerV, factors, products+traces, assembly, planning; launches."""
-        out = np.zeros(6)
-        L.lib().slaph_engine_timings(self._h, L.dptr(out), 6)
+        """ms: VdaggerV, factors, products+traces, assembly, planning; launches;
+        the trace kernel alone (ms) and its launch count."""
+        out = np.zeros(8)
+        L.lib().slaph_engine_timings(self._h, L.dptr(out), 8)
         return out
 
     def stats(self):
