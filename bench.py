@@ -43,7 +43,7 @@ UNIT = "s/gauge-config"
 # from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum of one
 # launch divided by its trace entries) on the 16^3x32 Nev=64 pipi case, keyed
 # by dilE; the kernel's traffic scales with its trace entries.
-NCU_TRACE_DRAM_BYTES_PER_ENTRY = {}
+NCU_TRACE_DRAM_BYTES_PER_ENTRY = {8: 2280.0}
 
 
 def load_peaks():

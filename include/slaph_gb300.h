@@ -45,9 +45,11 @@ extern "C" {
 enum slaph_precision {
   SLAPH_FP64 = 0,  /* every product in FP64                                   */
   SLAPH_MIXED = 1  /* VdaggerV as split-BF16 tensor-core products with exact
-                      FP32 partial sums; diluted traces as compensated
-                      double-float (2 x FP32) dot products; factors, products
-                      and the correlator sums in FP64                          */
+                      FP32 partial sums; diluted factors, factor products and
+                      traces in compensated double-float (2 x FP32)
+                      arithmetic; terms and correlator sums in FP64.
+                      Correlators agree with SLAPH_FP64 to about 1e-12
+                      relative (tested at 1e-10)                                */
 };
 
 enum slaph_accumulator {
