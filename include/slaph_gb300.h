@@ -44,8 +44,9 @@ extern "C" {
 /* ---- enums ------------------------------------------------------------- */
 enum slaph_precision {
   SLAPH_FP64 = 0,  /* every product in FP64                                   */
-  SLAPH_MIXED = 1  /* VdaggerV as split-BF16 tensor-core products with exact
-                      FP32 partial sums; diluted factors, factor products and
+  SLAPH_MIXED = 1  /* VdaggerV and the traces of dense trace groups as
+                      split-BF16 tensor-core products with exact FP32 partial
+                      sums; diluted factors, factor products and the other
                       traces in compensated double-float (2 x FP32)
                       arithmetic; terms and correlator sums in FP64.
                       Correlators agree with SLAPH_FP64 to about 1e-12
@@ -253,8 +254,10 @@ int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt);
  * measured with CUDA events on the engine stream.  out[0] VdaggerV,
  * out[1] factors Q0/Q1/Q2, out[2] products + traces, out[3] assembly,
  * out[4] host planning (wall clock), out[5] kernel launches issued,
- * out[6] the trace kernel alone (summed over its launches), out[7] its
- * launch count.  Returns the number of values written (<= n). */
+ * out[6] the per-entry trace kernel alone (summed over its launches), out[7]
+ * its launch count, out[8] the tensor-core trace GEMM (mixed precision),
+ * out[9] its launch count, out[10] the slicing of its operands.  Returns the
+ * number of values written (<= n, at most 12). */
 int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
 
 /* VdaggerV of one operator on one timeslice for callers that cannot let a
@@ -280,7 +283,9 @@ int slaph_vdaggerv_noalloc(const slaph_dims *dims, const double *V_t, const int3
 
 /* Device-resident statistics of the last contract: out[0] factors built,
  * out[1] products, out[2] traces, out[3] correlator terms, out[4] flops of
- * the factor stage, out[5] flops of products+traces. */
+ * the factor stage, out[5] flops of products+traces, out[6] trace entries
+ * computed after merging lists with equal operands, out[7] of those, the
+ * entries in dense groups (tensor-core GEMMs in mixed precision). */
 int slaph_engine_stats(const slaph_engine *eng, double *out, int n);
 
 #ifdef __cplusplus

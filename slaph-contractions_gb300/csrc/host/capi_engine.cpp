@@ -82,7 +82,7 @@ int slaph_engine_timings(const slaph_engine *eng, double *out, int n) {
     slaph::set_last_error("invalid argument");
     return -1;
   }
-  int const m = n < 8 ? n : 8;
+  int const m = n < 12 ? n : 12;
   for (int i = 0; i < m; ++i) out[i] = eng->e->timings[i];
   return m;
 }
@@ -92,7 +92,7 @@ int slaph_engine_stats(const slaph_engine *eng, double *out, int n) {
     slaph::set_last_error("invalid argument");
     return -1;
   }
-  int const m = n < 6 ? n : 6;
+  int const m = n < 8 ? n : 8;
   for (int i = 0; i < m; ++i) out[i] = eng->e->stats[i];
   return m;
 }

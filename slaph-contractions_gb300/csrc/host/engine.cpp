@@ -48,6 +48,9 @@ namespace {
 
 // Upper bound of the split-precision VdaggerV scratch (timeslice batches).
 constexpr size_t kTcScratchCap = 24ULL << 30;
+// Smallest batch capacity of the tensor-core traces (the VdaggerV scratch is
+// reused when it is larger).
+constexpr size_t kTraceScratchMin = 1ULL << 30;
 
 template <typename T>
 void upload(DevBuf &b, std::vector<T> const &v, cudaStream_t s) {
@@ -96,6 +99,8 @@ Engine::Engine(slaph_dims const &d) : dims_(d) {
 Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (auto &e : ev_)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : tc_ev_)
     if (e) cudaEventDestroy(e);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -251,6 +256,8 @@ void Engine::prepare_schedule(slaph_plan const *plan, int bp) {
     upload(wb->prods, w.prods, stream_);
     upload(wb->lists, w.lists, stream_);
     upload(wb->terms, w.terms, stream_);
+    upload(wb->unique, w.unique_lists, stream_);
+    upload(wb->residual, w.residual_lists, stream_);
     // Stable counting sort of the terms by output (request, dt) gives the
     // per-output summation order of Diagram::assemble.
     int64_t const n_out = s.n_outputs * Lt;
@@ -286,6 +293,123 @@ void Engine::prepare_schedule(slaph_plan const *plan, int bp) {
   sched_ = std::move(ds);
   sched_plan_ = plan;
   sched_bp_ = bp;
+}
+
+// Tensor-core plan of the dense trace groups: per group, one A region per
+// distinct entry row i (the matrices a + i of all A groups) and one B region
+// per distinct entry column j; one GEMM per entry (i, j) over its regions, cut
+// into 64 x 80 tiles.  Groups are packed into batches of at most the scratch
+// capacity (a group larger than that raises it).
+void Engine::prepare_trace_tc(DeviceSchedule &ds) {
+  if (ds.tc_ready) return;
+  Schedule const &s = ds.s;
+  int32_t const eds = s.eds;
+  // Bytes of one 64-row A tile stream and one 80-column B tile stream.
+  int64_t const a_tile = static_cast<int64_t>(dev::trace_tc_a_bytes(1, eds));
+  int64_t const b_tile = static_cast<int64_t>(dev::trace_tc_b_bytes(1, eds));
+  size_t cap = std::max(tc_scratch_.size(), kTraceScratchMin);
+  for (auto const &w : s.waves)
+    for (auto const &g : w.groups) {
+      auto const &sh = s.shapes[g.shape];
+      std::vector<int32_t> is(sh.i.begin(), sh.i.end()), js(sh.j.begin(), sh.j.end());
+      std::sort(is.begin(), is.end());
+      std::sort(js.begin(), js.end());
+      size_t const ni = std::unique(is.begin(), is.end()) - is.begin();
+      size_t const nj = std::unique(js.begin(), js.end()) - js.begin();
+      cap = std::max(cap, ni * dev::trace_tc_a_bytes(g.n_a, eds) +
+                              nj * dev::trace_tc_b_bytes(g.n_b, eds));
+    }
+  size_t need = 0;
+  int64_t max_expo = 0;
+  for (size_t wi = 0; wi < s.waves.size(); ++wi) {
+    Wave const &w = s.waves[wi];
+    auto &wb = *ds.waves[wi];
+    std::vector<dev::TrSlice> av, bv;
+    std::vector<dev::TrTile> tiles;
+    wb.tc_batches.clear();
+    DeviceSchedule::TcBatch cur{0, 0, 0, 0, 0, 0};
+    size_t used = 0;
+    int64_t expo = 0;
+    auto close = [&] {
+      cur.n_a = static_cast<int64_t>(av.size()) - cur.a_off;
+      cur.n_b = static_cast<int64_t>(bv.size()) - cur.b_off;
+      cur.n_tiles = static_cast<int64_t>(tiles.size()) - cur.tile_off;
+      if (cur.n_tiles > 0) wb.tc_batches.push_back(cur);
+      need = std::max(need, used);
+      max_expo = std::max(max_expo, expo);
+      cur = {static_cast<int64_t>(av.size()), 0, static_cast<int64_t>(bv.size()), 0,
+             static_cast<int64_t>(tiles.size()), 0};
+      used = 0;
+      expo = 0;
+    };
+    for (auto const &g : w.groups) {
+      auto const &sh = s.shapes[g.shape];
+      std::vector<int32_t> is(sh.i.begin(), sh.i.end()), js(sh.j.begin(), sh.j.end());
+      std::sort(is.begin(), is.end());
+      is.erase(std::unique(is.begin(), is.end()), is.end());
+      std::sort(js.begin(), js.end());
+      js.erase(std::unique(js.begin(), js.end()), js.end());
+      size_t const ab = dev::trace_tc_a_bytes(g.n_a, eds), bb = dev::trace_tc_b_bytes(g.n_b, eds);
+      size_t const gb = is.size() * ab + js.size() * bb;
+      if (used > 0 && used + gb > cap) close();
+      // Regions and exponents of this group, by operand index.
+      size_t const ni = static_cast<size_t>(is.back()) + 1, nj = static_cast<size_t>(js.back()) + 1;
+      std::vector<int64_t> a_reg(ni, -1), b_reg(nj, -1), a_exp(ni, -1), b_exp(nj, -1);
+      for (int32_t i : is) {
+        a_reg[i] = static_cast<int64_t>(used);
+        a_exp[i] = expo;
+        for (int32_t ia = 0; ia < g.n_a; ++ia)
+          av.push_back({static_cast<int64_t>(used), w.group_bases[g.a_off + ia] + i, ia,
+                        static_cast<int32_t>(expo + ia), 0});
+        used += ab;
+        expo += g.n_a;
+      }
+      for (int32_t j : js) {
+        b_reg[j] = static_cast<int64_t>(used);
+        b_exp[j] = expo;
+        for (int32_t ib = 0; ib < g.n_b; ++ib)
+          bv.push_back({static_cast<int64_t>(used), w.group_bases[g.b_off + ib] + j, ib,
+                        static_cast<int32_t>(expo + ib), 0});
+        used += bb;
+        expo += g.n_b;
+      }
+      // GEMM tiles, entries in order of their A region (consecutive tiles share
+      // operand streams in L2).
+      int64_t const n_e = static_cast<int64_t>(sh.i.size());
+      std::vector<int64_t> eo(n_e);
+      std::iota(eo.begin(), eo.end(), 0);
+      std::stable_sort(eo.begin(), eo.end(),
+                       [&](int64_t x, int64_t y) { return sh.i[x] < sh.i[y]; });
+      int32_t const mts = (g.n_a + dev::kTrTileRows - 1) / dev::kTrTileRows;
+      int32_t const nts = (g.n_b + dev::kTrTileCols - 1) / dev::kTrTileCols;
+      int64_t const plane = static_cast<int64_t>(g.n_a) * g.n_b;
+      for (int64_t e : eo) {
+        int32_t const i = sh.i[e], j = sh.j[e];
+        for (int32_t mt = 0; mt < mts; ++mt)
+          for (int32_t nt = 0; nt < nts; ++nt) {
+            dev::TrTile t{};
+            t.a_src = a_reg[i] + static_cast<int64_t>(mt) * a_tile;
+            t.b_src = b_reg[j] + static_cast<int64_t>(nt) * b_tile;
+            t.out = g.val_base + e * plane + static_cast<int64_t>(nt) * dev::kTrTileCols * g.n_a +
+                    static_cast<int64_t>(mt) * dev::kTrTileRows;
+            t.ea = static_cast<int32_t>(a_exp[i] + mt * dev::kTrTileRows);
+            t.eb = static_cast<int32_t>(b_exp[j] + nt * dev::kTrTileCols);
+            t.rows = std::min(dev::kTrTileRows, g.n_a - mt * dev::kTrTileRows);
+            t.cols = std::min(dev::kTrTileCols, g.n_b - nt * dev::kTrTileCols);
+            t.ld = g.n_a;
+            tiles.push_back(t);
+          }
+      }
+    }
+    close();
+    upload(wb.tc_a, av, stream_);
+    upload(wb.tc_b, bv, stream_);
+    upload(wb.tc_tiles, tiles, stream_);
+    SLAPH_CK(cudaStreamSynchronize(stream_));
+  }
+  ds.tc_scratch = need;
+  ds.tc_expo = max_expo;
+  ds.tc_ready = true;
 }
 
 void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
@@ -385,8 +509,15 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   int64_t const n_run = std::max<int64_t>(1, s.n_outputs * dims_.Lt);
   running_.reserve(sizeof(double2) * n_run);
   SLAPH_CK(cudaMemsetAsync(running_.as<void>(), 0, sizeof(double2) * n_run, stream_));
-  double t_pt = 0, t_as = 0, t_tr = 0;
-  int64_t n_tr = 0;
+  double t_pt = 0, t_as = 0, t_tr = 0, t_sl = 0, t_gm = 0;
+  int64_t n_tr = 0, n_gm = 0;
+  if (mixed) {
+    prepare_trace_tc(ds);
+    tc_scratch_.reserve(std::max<size_t>(1, ds.tc_scratch));
+    tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, ds.tc_expo));
+    err_.reserve(sizeof(int));
+    SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
+  }
   for (size_t wi = 0; wi < s.waves.size(); ++wi) {
     Wave const &w = s.waves[wi];
     auto &wb = *ds.waves[wi];
@@ -402,27 +533,56 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
       else
         launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
     }
+    int64_t const n_res = static_cast<int64_t>(w.residual_lists.size());
+    int64_t const n_uni = static_cast<int64_t>(w.unique_lists.size());
     SLAPH_CK(cudaEventRecord(ev_[5], stream_));
     if (mixed) {
       values_df_.reserve(sizeof(float4) * std::max<int64_t>(1, s.max_values));
-      launch(dev::traces_df(values_df_.as<float4>(), wb.lists.as<dev::TraceList>(),
-                            static_cast<int64_t>(w.lists.size()), ds.shape_i.as<int32_t>(),
-                            ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
-                            df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds, stream_),
-             "traces_df");
+      if (n_res > 0)
+        launch(dev::traces_df(values_df_.as<float4>(), wb.lists.as<dev::TraceList>(),
+                              wb.residual.as<int32_t>(), n_res, ds.shape_i.as<int32_t>(),
+                              ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
+                              df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds, stream_),
+               "traces_df");
       SLAPH_CK(cudaEventRecord(ev_[6], stream_));
-      launch(dev::df_values_to_fp64(values_.as<double2>(), values_df_.as<float4>(), w.n_values,
-                                    stream_),
-             "df_values_to_fp64");
+      int64_t const gv = w.n_group_values;
+      if (w.n_values > gv)
+        launch(dev::df_values_to_fp64(values_.as<double2>() + gv, values_df_.as<float4>() + gv,
+                                      w.n_values - gv, stream_),
+               "df_values_to_fp64");
+      // Dense groups on the tensor cores: slice, then GEMM, per batch.
+      while (tc_ev_.size() < 3 * wb.tc_batches.size()) {
+        cudaEvent_t e = nullptr;
+        SLAPH_CK(cudaEventCreate(&e));
+        tc_ev_.push_back(e);
+      }
+      for (size_t bi = 0; bi < wb.tc_batches.size(); ++bi) {
+        auto const &b = wb.tc_batches[bi];
+        SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi], stream_));
+        cuda_check(dev::trace_tc_slice(tc_scratch_.as<uint8_t>(), tr_expo_.as<int32_t>(),
+                                       wb.tc_a.as<dev::TrSlice>() + b.a_off, b.n_a,
+                                       wb.tc_b.as<dev::TrSlice>() + b.b_off, b.n_b,
+                                       df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds,
+                                       stream_),
+                   "trace_tc_slice");
+        launches_ += (b.n_a > 0 ? 1 : 0) + (b.n_b > 0 ? 1 : 0);
+        SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 1], stream_));
+        launch(dev::trace_tc_gemm(values_.as<double2>(), tc_scratch_.as<uint8_t>(),
+                                  tr_expo_.as<int32_t>(), wb.tc_tiles.as<dev::TrTile>() + b.tile_off,
+                                  b.n_tiles, eds, err_.as<int>(), stream_),
+               "trace_tc_gemm");
+        SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 2], stream_));
+      }
     } else {
-      launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
-                         static_cast<int64_t>(w.lists.size()), ds.shape_i.as<int32_t>(),
-                         ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
-                         slots_.as<double2>(), eds, w.n_values, stream_),
-             "traces");
+      if (n_uni > 0)
+        launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
+                           wb.unique.as<int32_t>(), n_uni, ds.shape_i.as<int32_t>(),
+                           ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
+                           slots_.as<double2>(), eds, stream_),
+               "traces");
       SLAPH_CK(cudaEventRecord(ev_[6], stream_));
     }
-    bool const traced = !w.lists.empty();
+    bool const traced = mixed ? n_res > 0 : n_uni > 0;
     SLAPH_CK(cudaEventRecord(ev_[3], stream_));
     launch(dev::terms(term_val_.as<double2>(), wb.terms.as<dev::Term>(),
                       static_cast<int64_t>(w.terms.size()), wb.lists.as<dev::TraceList>(),
@@ -442,6 +602,12 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
       t_tr += elapsed_ms(ev_[5], ev_[6]);
       ++n_tr;
     }
+    if (mixed)
+      for (size_t bi = 0; bi < wb.tc_batches.size(); ++bi) {
+        t_sl += elapsed_ms(tc_ev_[3 * bi], tc_ev_[3 * bi + 1]);
+        t_gm += elapsed_ms(tc_ev_[3 * bi + 1], tc_ev_[3 * bi + 2]);
+        ++n_gm;
+      }
   }
   timings[2] = t_pt;
   timings[3] = t_as;
@@ -449,6 +615,16 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   timings[5] = static_cast<double>(launches_);
   timings[6] = t_tr;
   timings[7] = static_cast<double>(n_tr);
+  timings[8] = t_gm;
+  timings[9] = static_cast<double>(n_gm);
+  timings[10] = t_sl;
+  if (mixed) {
+    int code = 0;
+    SLAPH_CK(cudaMemcpy(&code, err_.as<void>(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (code != 0)
+      throw TimeoutError("tensor-core traces: a bounded device wait gave up (stage " +
+                         std::to_string(code) + ")");
+  }
 
   // ---- output: C[t] = correlator[t][i] / Lt (src/Diagram.cpp:141-143)
   std::vector<double2> host(static_cast<size_t>(s.n_outputs * dims_.Lt));
@@ -461,6 +637,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     corr_out[2 * i] = host[i].x / inv;
     corr_out[2 * i + 1] = host[i].y / inv;
   }
+  stats[6] = static_cast<double>(s.n_unique_entries);
+  stats[7] = static_cast<double>(s.n_group_entries);
   stats[0] = static_cast<double>(s.q0.size() + s.q1.size() + s.q2.size());
   stats[1] = static_cast<double>(s.n_prods);
   stats[2] = static_cast<double>(s.n_trace_entries);

@@ -44,12 +44,22 @@ struct DeviceSchedule {
   Schedule s;
   DevBuf q0m, q1r, q2m, q0, q1, q2;
   DevBuf shape_i, shape_j, shape_mask, shape_off;
+  // Dense trace groups of a wave cut into batches that fit the tensor-core
+  // scratch buffer: slicing items and GEMM tiles per batch.
+  struct TcBatch {
+    int64_t a_off, n_a, b_off, n_b, tile_off, n_tiles;
+  };
   struct WaveBufs {
-    DevBuf prods, lists, terms, seg_out, seg_off, idx;
+    DevBuf prods, lists, terms, seg_out, seg_off, idx, unique, residual;
     int64_t n_seg = 0;
+    DevBuf tc_a, tc_b, tc_tiles;
+    std::vector<TcBatch> tc_batches;
   };
   std::vector<std::unique_ptr<WaveBufs>> waves;
   double plan_seconds = 0;
+  bool tc_ready = false;
+  size_t tc_scratch = 0;   // bytes of scratch the batches need
+  int64_t tc_expo = 0;     // exponents per batch (maximum)
 };
 
 class Engine {
@@ -66,8 +76,8 @@ class Engine {
   void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
                 double *corr_out);
 
-  double timings[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  double stats[6] = {0, 0, 0, 0, 0, 0};
+  double timings[12] = {};
+  double stats[8] = {};
 
  private:
   slaph_dims dims_;
@@ -75,6 +85,7 @@ class Engine {
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev_[8] = {};
+  std::vector<cudaEvent_t> tc_ev_;  // three per tensor-core trace batch
 
   DevBuf V_, peram_, noise_, phase_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
   std::vector<slaph_vdv_op> ops_;
@@ -83,7 +94,7 @@ class Engine {
   int64_t launches_ = 0;
 
   // Working buffers of the contraction.
-  DevBuf slots_, df_slots_, df_slots_t_, values_, values_df_, term_val_, running_;
+  DevBuf slots_, df_slots_, df_slots_t_, values_, values_df_, term_val_, running_, tr_expo_;
 
   std::unique_ptr<DeviceSchedule> sched_;
   slaph_plan const *sched_plan_ = nullptr;
@@ -91,6 +102,7 @@ class Engine {
 
   int64_t peram_elems() const;
   void prepare_schedule(slaph_plan const *plan, int single_block_pair);
+  void prepare_trace_tc(DeviceSchedule &ds);
   void launch(cudaError_t e, char const *what) {
     cuda_check(e, what);
     ++launches_;

@@ -2,8 +2,12 @@
 #include "schedule.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
+#include <exception>
 #include <map>
+#include <mutex>
+#include <thread>
 #include <tuple>
 #include <unordered_map>
 
@@ -201,6 +205,32 @@ class Builder {
         if (l.b_base != INT32_MIN) l.b_base = fix(l.b_base);
         else l.b_base = -1;
       }
+    }
+    // Waves are grouped independently, in parallel.
+    {
+      std::atomic<size_t> next{0};
+      std::exception_ptr err;
+      std::mutex mu;
+      size_t const nw = s_.waves.size();
+      unsigned const hw = std::max(1u, std::thread::hardware_concurrency());
+      std::vector<std::thread> pool;
+      for (unsigned k = 0; k < std::min<size_t>(hw, nw); ++k)
+        pool.emplace_back([&] {
+          for (size_t i; (i = next++) < nw;) {
+            try {
+              group_lists(s_.waves[i]);
+            } catch (...) {
+              std::lock_guard<std::mutex> g(mu);
+              if (!err) err = std::current_exception();
+            }
+          }
+        });
+      for (auto &t : pool) t.join();
+      if (err) std::rethrow_exception(err);
+    }
+    for (auto &w : s_.waves) {
+      s_.n_unique_entries += unique_entries(w);
+      s_.n_group_entries += w.n_group_entries;
       s_.max_prod_slots = std::max(s_.max_prod_slots, w.n_prod_slots);
       s_.max_values = std::max(s_.max_values, w.n_values);
       s_.max_terms = std::max<int64_t>(s_.max_terms, static_cast<int64_t>(w.terms.size()));
@@ -217,6 +247,136 @@ class Builder {
                               s_.q1.size() * 16.0 * dilE * dilE * nev +
                               s_.q2m.size() * 16.0 * dilE * nev * nev +
                               s_.q2.size() * 64.0 * dilE * dilE * nev);
+  }
+
+  int64_t unique_entries(Wave const &w) const {
+    int64_t n = 0;
+    for (int32_t l : w.unique_lists) n += static_cast<int64_t>(s_.shapes[w.lists[l].shape].i.size());
+    return n;
+  }
+
+  // Merges lists with equal operands, finds the dense trace groups and lays
+  // out the trace values: group values first (entry-major, B group, A group),
+  // then the residual lists one after another.
+  void group_lists(Wave &w) {
+    int64_t const n = static_cast<int64_t>(w.lists.size());
+    std::vector<int32_t> ord(n);
+    for (int64_t k = 0; k < n; ++k) ord[k] = static_cast<int32_t>(k);
+    auto key = [&](int32_t k) {
+      auto const &l = w.lists[k];
+      return std::make_tuple(l.shape, l.a_base, l.b_base);
+    };
+    std::sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) {
+      auto const kx = key(x), ky = key(y);
+      return kx != ky ? kx < ky : x < y;
+    });
+    // canonical[k]: the lowest-numbered list with the operands of list k.
+    std::vector<int32_t> canonical(n);
+    std::vector<int32_t> uniq;  // canonical lists in key order
+    for (int64_t p = 0; p < n; ++p) {
+      if (p > 0 && key(ord[p]) == key(ord[p - 1])) {
+        canonical[ord[p]] = canonical[ord[p - 1]];
+      } else {
+        canonical[ord[p]] = ord[p];
+        uniq.push_back(ord[p]);
+      }
+    }
+    // Runs of equal (shape, a_base) among the two-matrix lists: the B set of
+    // each A group, in increasing b_base.  A groups with equal (shape, B set)
+    // form a complete bipartite set.
+    struct Run {
+      int32_t shape, a;
+      int64_t begin, end;  // into uniq
+      uint64_t hash;
+    };
+    std::vector<Run> runs;
+    for (int64_t p = 0; p < static_cast<int64_t>(uniq.size());) {
+      auto const &l = w.lists[uniq[p]];
+      int64_t q = p;
+      uint64_t h = 1469598103934665603ULL;
+      while (q < static_cast<int64_t>(uniq.size()) && w.lists[uniq[q]].shape == l.shape &&
+             w.lists[uniq[q]].a_base == l.a_base) {
+        h = (h ^ static_cast<uint32_t>(w.lists[uniq[q]].b_base)) * 1099511628211ULL;
+        ++q;
+      }
+      if (l.b_base >= 0) runs.push_back({l.shape, l.a_base, p, q, h});
+      p = q;
+    }
+    auto same_set = [&](Run const &x, Run const &y) {
+      if (x.shape != y.shape || x.end - x.begin != y.end - y.begin || x.hash != y.hash)
+        return false;
+      for (int64_t u = 0; u < x.end - x.begin; ++u)
+        if (w.lists[uniq[x.begin + u]].b_base != w.lists[uniq[y.begin + u]].b_base)
+          return false;
+      return true;
+    };
+    std::vector<int32_t> run_ord(runs.size());
+    for (size_t k = 0; k < runs.size(); ++k) run_ord[k] = static_cast<int32_t>(k);
+    std::stable_sort(run_ord.begin(), run_ord.end(), [&](int32_t x, int32_t y) {
+      auto const &a = runs[x], &b = runs[y];
+      return std::make_tuple(a.shape, a.hash, a.end - a.begin) <
+             std::make_tuple(b.shape, b.hash, b.end - b.begin);
+    });
+    std::vector<char> in_group(n, 0);
+    w.groups.clear();
+    w.group_bases.clear();
+    int64_t val = 0;
+    for (size_t p = 0; p < run_ord.size();) {
+      size_t q = p + 1;
+      while (q < run_ord.size() && same_set(runs[run_ord[p]], runs[run_ord[q]])) ++q;
+      Run const &r0 = runs[run_ord[p]];
+      int32_t const n_a = static_cast<int32_t>(q - p);
+      int32_t const n_b = static_cast<int32_t>(r0.end - r0.begin);
+      if (n_a >= kMinGroupA && n_b >= kMinGroupB) {
+        TraceGroup g{};
+        g.shape = r0.shape;
+        g.n_a = n_a;
+        g.n_b = n_b;
+        g.a_off = static_cast<int64_t>(w.group_bases.size());
+        std::vector<int32_t> members(run_ord.begin() + p, run_ord.begin() + q);
+        std::sort(members.begin(), members.end(),
+                  [&](int32_t x, int32_t y) { return runs[x].a < runs[y].a; });
+        for (int32_t m : members) w.group_bases.push_back(runs[m].a);
+        g.b_off = static_cast<int64_t>(w.group_bases.size());
+        for (int64_t u = r0.begin; u < r0.end; ++u)
+          w.group_bases.push_back(w.lists[uniq[u]].b_base);
+        g.val_base = val;
+        int64_t const n_e = static_cast<int64_t>(s_.shapes[g.shape].i.size());
+        int64_t const plane = static_cast<int64_t>(n_a) * n_b;
+        for (int32_t ia = 0; ia < n_a; ++ia) {
+          Run const &r = runs[members[ia]];
+          for (int64_t u = r.begin; u < r.end; ++u) {
+            auto &l = w.lists[uniq[u]];
+            l.val_off = val + (u - r.begin) * n_a + ia;
+            l.stride = static_cast<int32_t>(plane);
+            in_group[uniq[u]] = 1;
+          }
+        }
+        val += n_e * plane;
+        w.n_group_entries += n_e * plane;
+        w.groups.push_back(g);
+      }
+      p = q;
+    }
+    w.n_group_values = val;
+    w.unique_lists.clear();
+    w.residual_lists.clear();
+    for (int64_t k = 0; k < n; ++k) {
+      if (canonical[k] != k) continue;
+      w.unique_lists.push_back(static_cast<int32_t>(k));
+      if (in_group[k]) continue;
+      w.residual_lists.push_back(static_cast<int32_t>(k));
+      auto &l = w.lists[k];
+      l.val_off = val;
+      l.stride = 1;
+      val += static_cast<int64_t>(s_.shapes[l.shape].i.size());
+    }
+    for (int64_t k = 0; k < n; ++k)
+      if (canonical[k] != k) {
+        w.lists[k].val_off = w.lists[canonical[k]].val_off;
+        w.lists[k].stride = w.lists[canonical[k]].stride;
+      }
+    w.n_values = val;
   }
 
   slaph_factor_index const &op(int type, int ql) const {
@@ -383,6 +543,7 @@ class Builder {
     tl.shape = shape;
     tl.a_base = a.base;
     tl.b_base = b ? b->base : INT32_MIN;
+    tl.stride = 1;
     tl.val_off = w_.n_values;
     w_.n_values += static_cast<int64_t>(s_.shapes[shape].i.size());
     w_.lists.push_back(tl);

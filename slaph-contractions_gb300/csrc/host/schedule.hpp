@@ -69,12 +69,25 @@ struct TraceShape {
 };
 
 // One diluted-trace list: operand lists start at matrix slots a_base / b_base
-// (b_base < 0 for single-matrix traces); its values occupy
-// [val_off, val_off + shape size) of the wave's trace-value array.
+// (b_base < 0 for single-matrix traces); the value of entry e is element
+// val_off + e * stride of the wave's trace-value array.
 struct TraceList {
   int32_t shape;
   int32_t a_base, b_base;
+  int32_t stride;
   int64_t val_off;
+};
+
+// Two-matrix trace lists of one shape whose operand groups form a complete
+// bipartite set: every A group (a_base) with every B group (b_base).  For each
+// entry (i, j) of the shape, the values of all n_a x n_b lists are one complex
+// matrix product sum_k A[a + i]_k B[b + j]^T_k, a GEMM of n_a x n_b dot
+// products.  The value of list (ia, ib), entry e, is at
+// val_base + e * n_a * n_b + ib * n_a + ia.
+struct TraceGroup {
+  int32_t shape, n_a, n_b, pad;
+  int64_t a_off, b_off;  // A bases at group_bases[a_off...], B at [b_off...]
+  int64_t val_base;
 };
 
 // resolve_request for one (request, slice pair): a combination of n trace
@@ -92,6 +105,14 @@ struct Wave {
   std::vector<int64_t> prod_level_off;  // prods of level k: [off[k], off[k+1])
   std::vector<TraceList> lists;
   int64_t n_values = 0;
+  // Lists that repeat the operands of an earlier list share its values.  Of
+  // the distinct lists, those in groups are dense GEMMs; the rest, residual,
+  // are computed entry by entry.  Group values come first: [0, n_group_values).
+  std::vector<TraceGroup> groups;
+  std::vector<int32_t> group_bases;
+  int64_t n_group_values = 0, n_group_entries = 0;
+  std::vector<int32_t> unique_lists;    // one list per distinct operand set
+  std::vector<int32_t> residual_lists;  // distinct lists outside groups
   std::vector<Term> terms;            // reference order within the block pair
   int64_t n_prod_slots = 0;           // product slots used (after factor slots)
   // Work of this wave (flops, 8 per complex multiply-add).
@@ -119,7 +140,13 @@ struct Schedule {
 
   double flops_factors = 0, flops_products = 0, flops_traces = 0;
   int64_t n_terms = 0, n_trace_entries = 0, n_prods = 0;
+  // Trace entries computed after merging repeated lists, and those in groups.
+  int64_t n_unique_entries = 0, n_group_entries = 0;
 };
+
+// Smallest operand-group counts for a dense trace group (GEMM tiles hold 64 A
+// and 80 B groups); smaller bipartite sets stay residual.
+constexpr int32_t kMinGroupA = 16, kMinGroupB = 16;
 
 // Builds the schedule; throws EmptyError with the reference's messages when a
 // random-vector combination is empty.  single_block_pair >= 0 restricts the

@@ -35,6 +35,7 @@ struct ProdInst {
 struct TraceList {
   int32_t shape;
   int32_t a_base, b_base;
+  int32_t stride;
   int64_t val_off;
 };
 struct Term {
@@ -98,12 +99,14 @@ cudaError_t q2(double2 *slots, Q2Inst const *inst, int64_t n, double2 const *q2m
 cudaError_t products(double2 *slots, ProdInst const *p, int64_t n, int32_t eds,
                      cudaStream_t stream);
 
-// Trace values of every entry of every list (factor_to_trace,
-// src/DilutedTrace.cpp:84-165).  shape_i/shape_j: entry operand indices,
+// Trace values of every entry of the lists lists[which[0..n_which)]
+// (factor_to_trace, src/DilutedTrace.cpp:84-165), entry e of list L at
+// values[L.val_off + e * L.stride].  shape_i/shape_j: entry operand indices,
 // shape_off: [n_shapes+1] offsets into them.
-cudaError_t traces(double2 *values, TraceList const *lists, int64_t n_lists,
-                   int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
-                   double2 const *slots, int32_t eds, int64_t n_entries, cudaStream_t stream);
+cudaError_t traces(double2 *values, TraceList const *lists, int32_t const *which,
+                   int64_t n_which, int32_t const *shape_i, int32_t const *shape_j,
+                   int64_t const *shape_off, double2 const *slots, int32_t eds,
+                   cudaStream_t stream);
 
 // Mixed path: matrices in double-float form (float4 = re hi, re lo, im hi,
 // im lo per complex), written as stored (dst_n) and transposed (dst_t); traces
@@ -125,12 +128,45 @@ cudaError_t factors_df(float4 *sn, float4 *st, float4 *q0m_buf, float4 *q1r_buf,
 cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int64_t n,
                         int32_t eds, cudaStream_t stream);
 // Trace values as double-float pairs (re_hi, re_lo, im_hi, im_lo) into
-// values_df, one entry per (list, shape entry).
-cudaError_t traces_df(float4 *values_df, TraceList const *lists, int64_t n_lists,
-                      int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
-                      float4 const *slots_n, float4 const *slots_t, int32_t eds,
-                      cudaStream_t stream);
-// values[i] = hi + lo of values_df[i], the FP64 trace values the terms read.
+// values_df, laid out as for traces().
+cudaError_t traces_df(float4 *values_df, TraceList const *lists, int32_t const *which,
+                      int64_t n_which, int32_t const *shape_i, int32_t const *shape_j,
+                      int64_t const *shape_off, float4 const *slots_n, float4 const *slots_t,
+                      int32_t eds, cudaStream_t stream);
+// Dense trace groups on the tensor cores (trace_tc.cu).  One matrix slot
+// sliced into the operand stream of a GEMM region:
+struct TrSlice {
+  int64_t dst;   // byte offset of the region in the scratch buffer
+  int32_t slot;  // matrix slot
+  int32_t row;   // complex row (A region) or column (B region) of the matrix
+  int32_t expo;  // index of the matrix's exponent in the exponent array
+  int32_t pad;
+};
+// One output tile of 64 A groups x 80 B groups of one (group, entry) GEMM.
+struct TrTile {
+  int64_t a_src, b_src;  // byte offsets of the tile's A and B operand streams
+  int64_t out;           // value index of tile row 0, column 0
+  int32_t ea, eb;        // exponent indices of tile row 0 and column 0
+  int32_t rows, cols;    // valid rows (<= 64) and columns (<= 80)
+  int32_t ld;            // value index distance between columns
+  int32_t pad;
+};
+constexpr int32_t kTrTileRows = 64, kTrTileCols = 80;
+int64_t trace_tc_k_tiles(int32_t eds);
+size_t trace_tc_a_bytes(int32_t rows, int32_t eds);  // A region of `rows` matrices
+size_t trace_tc_b_bytes(int32_t cols, int32_t eds);  // B region of `cols` matrices
+// Slices the A matrices (natural layout, conjugated) and B matrices
+// (transposed layout) of a batch into their regions of `scratch`.
+cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSlice const *a_items, int64_t n_a,
+                           TrSlice const *b_items, int64_t n_b, float4 const *slots_n,
+                           float4 const *slots_t, int32_t eds, cudaStream_t stream);
+// The GEMM tiles of a batch; FP64 trace values into `values`.
+cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
+                          TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,
+                          cudaStream_t stream);
+
+// values[i] = hi + lo of values_df[i] for i < n_values, the FP64 trace values
+// the terms read.
 cudaError_t df_values_to_fp64(double2 *values, float4 const *values_df, int64_t n_values,
                               cudaStream_t stream);
 

@@ -406,11 +406,12 @@ __global__ void __launch_bounds__(256) product_kernel(double2 *slots, ProdInst c
 // factor_to_trace, src/DilutedTrace.cpp:84-165: tr(L R) per entry (or tr(F)).
 // One CTA per list, one warp per entry, one lane per row.
 __global__ void __launch_bounds__(256) trace_kernel(double2 *values, TraceList const *lists,
+                                                    int32_t const *which,
                                                     int32_t const *shape_i,
                                                     int32_t const *shape_j,
                                                     int64_t const *shape_off,
                                                     double2 const *slots, int32_t eds) {
-  TraceList const L = lists[blockIdx.x];
+  TraceList const L = lists[which[blockIdx.x]];
   int64_t const off = shape_off[L.shape];
   int const n = static_cast<int>(shape_off[L.shape + 1] - off);
   int const warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -438,7 +439,7 @@ __global__ void __launch_bounds__(256) trace_kernel(double2 *values, TraceList c
       acc.x += __shfl_down_sync(0xffffffffu, acc.x, s);
       acc.y += __shfl_down_sync(0xffffffffu, acc.y, s);
     }
-    if (lane == 0) values[L.val_off + e] = acc;
+    if (lane == 0) values[L.val_off + static_cast<int64_t>(e) * L.stride] = acc;
   }
 }
 
@@ -457,11 +458,12 @@ __global__ void term_kernel(double2 *term_val, Term const *terms, int64_t n,
   int64_t const o0 = shape_off[L0.shape];
   int64_t const n0 = shape_off[L0.shape + 1] - o0;
   double2 const *x0 = values + L0.val_off;
+  int64_t const s0 = L0.stride;
   uint16_t const *m0 = shape_mask + o0;
   double2 res;
   if (t.n == 1) {
     Acc a(kahan);
-    for (int64_t e = 0; e < n0; ++e) a.add(x0[e]);
+    for (int64_t e = 0; e < n0; ++e) a.add(x0[e * s0]);
     double2 const v = a.value();
     res = make_double2(v.x / static_cast<double>(n0), v.y / static_cast<double>(n0));
   } else {
@@ -469,6 +471,7 @@ __global__ void term_kernel(double2 *term_val, Term const *terms, int64_t n,
     int64_t const o1 = shape_off[L1.shape];
     int64_t const n1 = shape_off[L1.shape + 1] - o1;
     double2 const *x1 = values + L1.val_off;
+    int64_t const s1 = L1.stride;
     uint16_t const *m1 = shape_mask + o1;
     int64_t num = 0;
     Acc result(kahan);
@@ -477,26 +480,27 @@ __global__ void term_kernel(double2 *term_val, Term const *terms, int64_t n,
         Acc rs(kahan);
         for (int64_t r = 0; r < n1; ++r) {
           if ((m0[l] & m1[r]) != 0u) continue;
-          rs.add(x1[r]);
+          rs.add(x1[r * s1]);
           ++num;
         }
-        result.add(cmul(x0[l], rs.value()));
+        result.add(cmul(x0[l * s0], rs.value()));
       }
     } else {
       TraceList const L2 = lists[t.list[2]];
       int64_t const o2 = shape_off[L2.shape];
       int64_t const n2 = shape_off[L2.shape + 1] - o2;
       double2 const *x2 = values + L2.val_off;
+      int64_t const s2 = L2.stride;
       uint16_t const *m2 = shape_mask + o2;
       for (int64_t l = 0; l < n0; ++l)
         for (int64_t m = 0; m < n1; ++m) {
           Acc rs(kahan);
           for (int64_t r = 0; r < n2; ++r) {
             if ((m0[l] & m1[m] & m2[r]) != 0u) continue;
-            rs.add(x2[r]);
+            rs.add(x2[r * s2]);
             ++num;
           }
-          result.add(cmul(cmul(x0[l], x1[m]), rs.value()));
+          result.add(cmul(cmul(x0[l * s0], x1[m * s1]), rs.value()));
         }
     }
     double2 const v = result.value();
@@ -664,13 +668,13 @@ cudaError_t products(double2 *slots, ProdInst const *p, int64_t n, int32_t eds,
   return cudaGetLastError();
 }
 
-cudaError_t traces(double2 *values, TraceList const *lists, int64_t n_lists,
-                   int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
-                   double2 const *slots, int32_t eds, int64_t, cudaStream_t stream) {
-  if (n_lists == 0) return cudaSuccess;
-  trace_kernel<<<static_cast<unsigned>(n_lists), 256, 0, stream>>>(values, lists, shape_i,
-                                                                   shape_j, shape_off, slots,
-                                                                   eds);
+cudaError_t traces(double2 *values, TraceList const *lists, int32_t const *which,
+                   int64_t n_which, int32_t const *shape_i, int32_t const *shape_j,
+                   int64_t const *shape_off, double2 const *slots, int32_t eds,
+                   cudaStream_t stream) {
+  if (n_which == 0) return cudaSuccess;
+  trace_kernel<<<static_cast<unsigned>(n_which), 256, 0, stream>>>(
+      values, lists, which, shape_i, shape_j, shape_off, slots, eds);
   return cudaGetLastError();
 }
 
@@ -756,12 +760,13 @@ __device__ __forceinline__ void df_warp_sum(DfAcc &a) {
 }
 
 __global__ void __launch_bounds__(256) trace_df_kernel(float4 *values, TraceList const *lists,
+                                                       int32_t const *which,
                                                        int32_t const *shape_i,
                                                        int32_t const *shape_j,
                                                        int64_t const *shape_off,
                                                        float4 const *slots_n,
                                                        float4 const *slots_t, int32_t eds) {
-  TraceList const L = lists[blockIdx.x];
+  TraceList const L = lists[which[blockIdx.x]];
   int64_t const off = shape_off[L.shape];
   int const n = static_cast<int>(shape_off[L.shape + 1] - off);
   int const warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -804,7 +809,9 @@ __global__ void __launch_bounds__(256) trace_df_kernel(float4 *values, TraceList
     }
     df_warp_sum(ar);
     df_warp_sum(ai);
-    if (lane == 0) values[L.val_off + e] = make_float4(ar.s, ar.c, ai.s, ai.c);
+    if (lane == 0)
+      values[L.val_off + static_cast<int64_t>(e) * L.stride] =
+          make_float4(ar.s, ar.c, ai.s, ai.c);
   }
 }
 
@@ -881,13 +888,13 @@ cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int
   return cudaGetLastError();
 }
 
-cudaError_t traces_df(float4 *values_df, TraceList const *lists, int64_t n_lists,
-                      int32_t const *shape_i, int32_t const *shape_j, int64_t const *shape_off,
-                      float4 const *slots_n, float4 const *slots_t, int32_t eds,
-                      cudaStream_t stream) {
-  if (n_lists == 0) return cudaSuccess;
-  trace_df_kernel<<<static_cast<unsigned>(n_lists), 256, 0, stream>>>(
-      values_df, lists, shape_i, shape_j, shape_off, slots_n, slots_t, eds);
+cudaError_t traces_df(float4 *values_df, TraceList const *lists, int32_t const *which,
+                      int64_t n_which, int32_t const *shape_i, int32_t const *shape_j,
+                      int64_t const *shape_off, float4 const *slots_n, float4 const *slots_t,
+                      int32_t eds, cudaStream_t stream) {
+  if (n_which == 0) return cudaSuccess;
+  trace_df_kernel<<<static_cast<unsigned>(n_which), 256, 0, stream>>>(
+      values_df, lists, which, shape_i, shape_j, shape_off, slots_n, slots_t, eds);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,143 @@
+// Dense diluted-trace groups on the tensor cores (tcgen05, sm_103a).
+//
+// factor_to_trace (src/DilutedTrace.cpp:84-138) computes tr(L R) =
+// sum_k L_k (R^T)_k over the (4 dilE)^2 entries k of the two factor matrices.
+// When the lists of one trace shape pair every A group with every B group, the
+// values of entry (i, j) of all lists are the complex matrix product
+//   T(ia, ib) = sum_k A[a_ia + i]_k B[b_ib + j]^T_k,
+// a GEMM with K = (4 dilE)^2.  It runs with the split-BF16 scheme of
+// tc_common.cuh: A rows are conj(A) (so that the conjugating form gives the
+// plain product), B columns are the transposed B matrices.
+//
+// Operands are double-float matrices (float4 (re_hi, re_lo, im_hi, im_lo)) in
+// the natural (A) and transposed (B) layouts.  trace_slice_kernel cuts one
+// matrix per CTA into the operand stream of its GEMM region, with the
+// matrix's exponent; trace_gemm_kernel computes one 64 x 80 complex output
+// tile per CTA and writes FP64 trace values: the 32 lanes of a warp hold 16
+// consecutive A groups (re, im) of one output column, so the stores of each
+// column are 256 contiguous bytes.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+#include "tc_common.cuh"
+
+namespace slaph {
+namespace dev {
+
+namespace {
+
+using namespace tc;
+
+constexpr int kSliceThreads = 128;
+
+// One matrix per CTA: exponent of its largest |re|, |im|, then its slices.
+template <bool kIsA>
+__global__ void __launch_bounds__(kSliceThreads)
+    trace_slice_kernel(uint8_t *scratch, int32_t *expo, TrSlice const *items,
+                       float4 const *slots, int32_t eds) {
+  TrSlice const it = items[blockIdx.x];
+  int64_t const ms = static_cast<int64_t>(eds) * eds;
+  int64_t const k_tiles = ms / (kTK / 2);
+  float4 const *src = slots + static_cast<int64_t>(it.slot) * ms;
+  double mx = 0;
+  for (int64_t m = threadIdx.x; m < ms; m += kSliceThreads) {
+    float4 const v = src[m];
+    double const re = static_cast<double>(v.x) + static_cast<double>(v.y);
+    double const im = static_cast<double>(v.z) + static_cast<double>(v.w);
+    mx = fmax(mx, fmax(fabs(re), fabs(im)));
+  }
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, s));
+  __shared__ double red[kSliceThreads / 32];
+  if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = mx;
+  __syncthreads();
+  mx = red[0];
+#pragma unroll
+  for (int w = 1; w < kSliceThreads / 32; ++w) mx = fmax(mx, red[w]);
+  int const e = expo_of_max(mx);
+  if (threadIdx.x == 0) expo[it.expo] = e;
+  uint8_t *region = scratch + it.dst;
+  for (int64_t m = threadIdx.x; m < ms; m += kSliceThreads) {
+    float4 const v = src[m];
+    double const re = static_cast<double>(v.x) + static_cast<double>(v.y);
+    double const im = static_cast<double>(v.z) + static_cast<double>(v.w);
+    if (kIsA)
+      put_a(region, k_tiles, it.row, m, make_double2(re, -im), e);
+    else
+      put_b(region, k_tiles, it.row, m, make_double2(re, im), e);
+  }
+}
+
+// FP64 trace values of one tile: value (r, c) = (hi + lo) 2^(e_r + e_c - 14)
+// at values[out + c * ld + r], component row & 1 (re, im).
+struct TraceEpilogue {
+  double *values;
+  int32_t const *expo;
+  TrTile t;
+  __device__ __forceinline__ void operator()(int row, float const (&hi)[kTN],
+                                             float const (&lo)[kTN]) const {
+    int const r = row / 2;
+    if (r >= t.rows) return;
+    int const er = expo[t.ea + r];
+    double *dst = values + 2 * (t.out + r) + (row & 1);
+#pragma unroll
+    for (int c = 0; c < kTN; ++c) {
+      if (c < t.cols)
+        dst[2 * static_cast<int64_t>(c) * t.ld] =
+            ldexp(static_cast<double>(hi[c]) + static_cast<double>(lo[c]),
+                  er + expo[t.eb + c] - 14);
+    }
+  }
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    trace_gemm_kernel(double2 *values, uint8_t const *scratch, int32_t const *expo,
+                      TrTile const *tiles, int32_t k_tiles, int *err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  TrTile const t = tiles[blockIdx.x];
+  TraceEpilogue epi{reinterpret_cast<double *>(values), expo, t};
+  ozaki_tile(smem, scratch + t.a_src, scratch + t.b_src, k_tiles, err, epi);
+}
+
+}  // namespace
+
+int64_t trace_tc_k_tiles(int32_t eds) {
+  return static_cast<int64_t>(eds) * eds / (kTK / 2);
+}
+size_t trace_tc_a_bytes(int32_t rows, int32_t eds) {
+  return static_cast<size_t>((rows + kTM / 2 - 1) / (kTM / 2)) * trace_tc_k_tiles(eds) * kStageA;
+}
+size_t trace_tc_b_bytes(int32_t cols, int32_t eds) {
+  return static_cast<size_t>((cols + kTN - 1) / kTN) * trace_tc_k_tiles(eds) * kStageB;
+}
+
+cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSlice const *a_items, int64_t n_a,
+                           TrSlice const *b_items, int64_t n_b, float4 const *slots_n,
+                           float4 const *slots_t, int32_t eds, cudaStream_t stream) {
+  if ((static_cast<int64_t>(eds) * eds) % (kTK / 2) != 0) return cudaErrorInvalidValue;
+  if (n_a > 0)
+    trace_slice_kernel<true><<<static_cast<unsigned>(n_a), kSliceThreads, 0, stream>>>(
+        scratch, expo, a_items, slots_n, eds);
+  if (n_b > 0)
+    trace_slice_kernel<false><<<static_cast<unsigned>(n_b), kSliceThreads, 0, stream>>>(
+        scratch, expo, b_items, slots_t, eds);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
+                          TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,
+                          cudaStream_t stream) {
+  if (n_tiles == 0) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(trace_gemm_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(kSmemBytes));
+  if (e != cudaSuccess) return e;
+  trace_gemm_kernel<<<static_cast<unsigned>(n_tiles), kThreads, kSmemBytes, stream>>>(
+      values, scratch, expo, tiles, static_cast<int32_t>(trace_tc_k_tiles(eds)), err);
+  return cudaGetLastError();
+}
+
+}  // namespace dev
+}  // namespace slaph

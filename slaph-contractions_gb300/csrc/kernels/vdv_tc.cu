@@ -1,203 +1,29 @@
 // Split-BF16 tensor-core VdaggerV (tcgen05, sm_103a).
 //
 // VdaggerV = V^H diag(phase) V (src/OperatorFactory.cpp:292-300) with FP64
-// inputs and an FP64-accurate result from BF16 tensor-core products:
-//
-// * Complex -> real.  With K' = 2 * 3L^3 interleaved (re, im), rows
-//   A'(2i) = (Re V_i, Im V_i), A'(2i+1) = (-Im V_i, Re V_i) and
-//   B(j) = (Re W_j, Im W_j), W = diag(phase) V, one real GEMM D = A' B^T gives
-//   D(2i, j) = Re(V_i^H W_j) and D(2i+1, j) = Im(V_i^H W_j).
-// * Exact split.  Every row is scaled by 2^-e (e: exponent of the column's
-//   largest |V|, the same for W since |phase| = 1) and cut into 6 signed slices
-//   of at most 8 bits: x = sum_p a_p 2^(-7-8(p-1)), a_p integer in [-128, 128],
-//   exact in BF16.  47 bits are kept.
-// * Exact FP32 accumulation.  Slice products a_p b_q (|.| <= 2^14) of the same
-//   scale level l = p + q are accumulated in one TMEM accumulator.  Over a chunk
-//   of 256 K' values the levels 2..5 stay below 2^24 and are exact; levels 6, 7
-//   (scale <= 2^-32) carry FP32 rounding far below the target.  21 pairs
-//   (p + q <= 7), 6 accumulators.
-// * Promotion.  After every chunk the 6 accumulators are read from TMEM and
-//   added, scaled by 2^-8(l-2), into a double-float (two FP32) accumulator in
-//   registers; FP64 units are not used in the loop.
+// inputs and an FP64-accurate result from BF16 tensor-core products, by the
+// split-BF16 scheme of tc_common.cuh: A' rows are the eigenvectors V_i, B
+// columns W_j = diag(phase) V_j, K' = 2 * 3L^3; rows are scaled by the
+// exponent of the eigenvector's largest |entry| (the same for W, |phase| = 1).
 //
 // Data path: slices are written once per timeslice (A) and per timeslice and
-// operator (B) to HBM, already in the tcgen05 K-major core-matrix layout, one
-// contiguous block per (tile, k-tile), and moved to shared memory by bulk
-// asynchronous copies (cp.async.bulk) completing on mbarriers.  Warp roles:
-// warp 4 issues the copies, warp 5 issues tcgen05.mma, warps 0-3 promote and
-// write the result.  Every mbarrier wait is bounded; on timeout the kernel
-// records an error code and winds down.
+// operator (B) to HBM, already in the tcgen05 core-matrix layout, and streamed
+// into shared memory by the GEMM (grid: m tiles x n tiles x operators x
+// timeslices of a batch).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
 
 #include "kernels.cuh"
+#include "tc_common.cuh"
 
 namespace slaph {
 namespace dev {
 
 namespace {
 
-constexpr int kSlices = 6;
-constexpr int kTM = 128;       // rows of A' per tile (64 eigenvectors x re/im)
-constexpr int kTN = 80;        // columns (eigenvectors) of B per tile
-constexpr int kTK = 32;        // K' per k-tile (bf16 elements)
-constexpr int kChunkKT = 8;    // k-tiles per exact chunk (256 K')
-constexpr int kStages = 2;
-constexpr uint32_t kABlk = kTM * kTK * 2;            // 8192 B
-constexpr uint32_t kBBlk = kTN * kTK * 2;            // 5120 B
-constexpr uint32_t kStageA = kSlices * kABlk;        // 49152 B
-constexpr uint32_t kStageB = kSlices * kBBlk;        // 30720 B
-constexpr uint32_t kStageBytes = kStageA + kStageB;  // 79872 B
-constexpr uint32_t kTmemCols = 512;
-constexpr int kLevels = 6;  // p + q = 2..7
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
-
-// byte offset of element (r, k) in a K-major, no-swizzle core-matrix tile with
-// 32 bf16 per row: core matrices of 8 rows x 16 B, adjacent along K at 128 B,
-// 8-row groups at 512 B.
-__host__ __device__ __forceinline__ uint32_t core_off(int r, int k) {
-  return ((r >> 3) * 4 + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
-}
-
-__device__ __forceinline__ uint32_t smem_u32(void const *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false (and *err = code) when the phase did not complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
-  long long const t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) {
-      atomicCAS(err, 0, code);
-      return false;
-    }
-  }
-  return true;
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, void const *src, uint32_t bytes,
-                                         uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-// Shared-memory matrix descriptor, K-major, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
-  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
-  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
-  d |= static_cast<uint64_t>(1) << 46;  // descriptor version (tcgen05)
-  return d;                             // base offset 0, no swizzle
-}
-// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, N = kTN, M = kTM.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
-                            (static_cast<uint32_t>(kTN >> 3) << 17) |
-                            (static_cast<uint32_t>(kTM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// Error-free x + y into (s, e) (Knuth's two-sum).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  float const bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-// ---------------------------------------------------------------- slicing
-// 64-bit fixed point of v relative to 2^e: F = round(v 2^(55-e)), |F| <= 2^55.
-__device__ __forceinline__ long long fixed55(double v, int e) {
-  long long const bits = __double_as_longlong(v);
-  int const ex = static_cast<int>((bits >> 52) & 0x7FF);
-  if (ex == 0) return 0;  // zero or subnormal: below 2^-1022, negligible here
-  long long m = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
-  // v = m 2^(ex - 1075); F = m 2^(ex - 1075 + 55 - e)
-  int const sh = ex - 1075 + 55 - e;
-  long long F;
-  if (sh >= 0) {
-    F = sh < 11 ? (m << sh) : (1LL << 62);  // sh >= 11 cannot occur for |v| <= 2^e
-  } else if (sh > -63) {
-    F = (m + (1LL << (-sh - 1))) >> (-sh);
-  } else {
-    F = 0;
-  }
-  return bits < 0 ? -F : F;
-}
-
-// Small integer (|a| <= 2^22) to the BF16 bits of the same value (exact for
-// |a| <= 256): float via the 1.5 * 2^23 bias, then the upper 16 bits.
-__device__ __forceinline__ uint16_t small_int_bf16(int a) {
-  float const f = __int_as_float(0x4B400000 + a) - 12582912.0f;
-  return static_cast<uint16_t>(__float_as_uint(f) >> 16);
-}
-
-__device__ __forceinline__ void slice6(long long F, uint16_t (&out)[kSlices]) {
-#pragma unroll
-  for (int p = 0; p < kSlices; ++p) {
-    int const sh = 48 - 8 * p;
-    long long const a = (F + (1LL << (sh - 1))) >> sh;
-    F -= a << sh;
-    out[p] = small_int_bf16(static_cast<int>(a));
-  }
-}
+using namespace tc;
 
 // Exponent e_i with max_x |V(x, i)| < 2^e_i per eigenvector (one block per i).
 __global__ void colmax_kernel(int32_t *expo, double2 const *Vt, Geometry g) {
@@ -232,25 +58,7 @@ __global__ void slice_a_kernel(uint16_t *out, double2 const *Vt, int32_t const *
   if (x >= static_cast<int64_t>(k_tiles) * (kTK / 2)) return;
   double2 v = make_double2(0, 0);
   if (x < g.dim_row) v = Vt[static_cast<int64_t>(i) * g.dim_row + x];
-  int const e = expo[i];
-  uint16_t sre[kSlices], sim[kSlices], snre[kSlices];
-  slice6(fixed55(v.x, e), sre);
-  slice6(fixed55(v.y, e), sim);
-  slice6(-fixed55(v.y, e), snre);
-  int const mt = i / (kTM / 2), r0 = 2 * (i % (kTM / 2));
-  int64_t const kt = x / (kTK / 2);
-  int const k = 2 * static_cast<int>(x % (kTK / 2));
-  uint8_t *blk = reinterpret_cast<uint8_t *>(out) +
-                 (static_cast<int64_t>(mt) * k_tiles + kt) * kSlices * kABlk;
-#pragma unroll
-  for (int p = 0; p < kSlices; ++p) {
-    uint8_t *b = blk + p * kABlk;
-    // row 2i: (Re, Im); row 2i+1: (-Im, Re)
-    *reinterpret_cast<uint32_t *>(b + core_off(r0, k)) =
-        static_cast<uint32_t>(sre[p]) | (static_cast<uint32_t>(sim[p]) << 16);
-    *reinterpret_cast<uint32_t *>(b + core_off(r0 + 1, k)) =
-        static_cast<uint32_t>(snre[p]) | (static_cast<uint32_t>(sre[p]) << 16);
-  }
+  put_a(reinterpret_cast<uint8_t *>(out), k_tiles, i, x, v, expo[i]);
 }
 
 // B slices of W = diag(phase_op) V: [op][n_tile][k_tile][slice][kTN x kTK].
@@ -267,201 +75,54 @@ __global__ void slice_b_kernel(uint16_t *out, double2 const *Vt, double2 const *
     double2 const ph = phase[static_cast<int64_t>(ops[o]) * (g.dim_row / 3) + x / 3];
     w = make_double2(ph.x * v.x - ph.y * v.y, ph.x * v.y + ph.y * v.x);
   }
-  int const e = expo[j];
-  uint16_t sre[kSlices], sim[kSlices];
-  slice6(fixed55(w.x, e), sre);
-  slice6(fixed55(w.y, e), sim);
-  int const nt = j / kTN, r = j % kTN;
-  int64_t const kt = x / (kTK / 2);
-  int const k = 2 * static_cast<int>(x % (kTK / 2));
-  uint8_t *blk = reinterpret_cast<uint8_t *>(out) +
-                 ((static_cast<int64_t>(o) * n_tiles + nt) * k_tiles + kt) * kSlices * kBBlk;
-#pragma unroll
-  for (int p = 0; p < kSlices; ++p)
-    *reinterpret_cast<uint32_t *>(blk + p * kBBlk + core_off(r, k)) =
-        static_cast<uint32_t>(sre[p]) | (static_cast<uint32_t>(sim[p]) << 16);
+  uint8_t *region = reinterpret_cast<uint8_t *>(out) +
+                    static_cast<int64_t>(o) * n_tiles * k_tiles * kStageB;
+  put_b(region, k_tiles, j, x, w, expo[j]);
 }
 
-// The GEMM: grid (m_tiles, n_tiles, n_ops * batch), 192 threads.  Batch slot b
-// (timeslice t0 + b) has its own A slices, B slices and exponents at stride
-// slot_bytes in the scratch buffer.
-__global__ void __launch_bounds__(192, 1)
+// Epilogue of one VdaggerV tile: D = (hi + lo) 2^(e_i + e_j - 14), rows
+// (2i, 2i+1) = (Re, Im) of VdaggerV(i, j), column-major nev x nev blocks.
+struct VdvEpilogue {
+  double *outd;
+  int32_t const *expo;
+  int i0, j0, nev;
+  __device__ __forceinline__ void operator()(int row, float const (&hi)[kTN],
+                                             float const (&lo)[kTN]) const {
+    int const i = i0 + row / 2;
+    if (i >= nev) return;
+    int const ei = expo[i];
+#pragma unroll
+    for (int jj = 0; jj < kTN; ++jj) {
+      int const j = j0 + jj;
+      if (j < nev) {
+        double const val = ldexp(static_cast<double>(hi[jj]) + static_cast<double>(lo[jj]),
+                                 ei + expo[j] - 14);
+        outd[2 * (i + static_cast<int64_t>(nev) * j) + (row & 1)] = val;
+      }
+    }
+  }
+};
+
+// The GEMM: grid (m_tiles, n_tiles, n_ops * batch), kThreads threads.  Batch
+// slot b (timeslice t0 + b) has its own A slices, B slices and exponents at
+// stride slot_bytes in the scratch buffer.
+__global__ void __launch_bounds__(kThreads, 1)
     ozaki_gemm_kernel(uint8_t const *scratch, size_t slot_bytes, size_t b_off, size_t e_off,
                       double2 *vdv, int32_t const *ops, int32_t n_ops, int32_t k_tiles,
                       int32_t n_tiles, int32_t t0, Geometry g, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages];
-  __shared__ __align__(8) uint64_t acc_full, acc_empty, done_bar;
-  __shared__ uint32_t tmem_slot;
-
-  int const warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   int const mt = blockIdx.x, nt = blockIdx.y;
   int const o = blockIdx.z % n_ops, slot = blockIdx.z / n_ops;
   int const t = t0 + slot;
   uint8_t const *sbase = scratch + slot * slot_bytes;
-  uint16_t const *A = reinterpret_cast<uint16_t const *>(sbase);
-  uint16_t const *B = reinterpret_cast<uint16_t const *>(sbase + b_off);
-  int32_t const *expo = reinterpret_cast<int32_t const *>(sbase + e_off);
-  int const n_chunks = (k_tiles + kChunkKT - 1) / kChunkKT;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(&full_bar[s], 1);
-      mbar_init(&empty_bar[s], 1);
-    }
-    mbar_init(&acc_full, 1);
-    mbar_init(&acc_empty, 4 * 32);
-    mbar_init(&done_bar, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(&tmem_slot)),
-                 "r"(kTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  uint32_t const tmem = tmem_slot;
-
-  uint8_t const *a_src = reinterpret_cast<uint8_t const *>(A) +
-                         static_cast<int64_t>(mt) * k_tiles * kStageA;
-  uint8_t const *b_src = reinterpret_cast<uint8_t const *>(B) +
-                         (static_cast<int64_t>(o) * n_tiles + nt) * k_tiles * kStageB;
-
-  if (warp == 4) {
-    if (lane == 0) {  // producer
-      for (int kt = 0; kt < k_tiles; ++kt) {
-        int const s = kt % kStages, use = kt / kStages;
-        if (kt >= kStages && !mbar_wait(&empty_bar[s], (use - 1) & 1, err, 1)) break;
-        uint8_t *dst = smem + s * kStageBytes;
-        mbar_expect_tx(&full_bar[s], kStageBytes);
-        bulk_g2s(dst, a_src + static_cast<int64_t>(kt) * kStageA, kStageA, &full_bar[s]);
-        bulk_g2s(dst + kStageA, b_src + static_cast<int64_t>(kt) * kStageB, kStageB,
-                 &full_bar[s]);
-      }
-    }
-  } else if (warp == 5) {
-    if (lane == 0) {  // MMA issuer
-      bool ok = true;
-      for (int c = 0; c < n_chunks && ok; ++c) {
-        if (c > 0 && !mbar_wait(&acc_empty, (c - 1) & 1, err, 2)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        uint32_t started = 0;
-        int const kt_end = min(k_tiles, (c + 1) * kChunkKT);
-        for (int kt = c * kChunkKT; kt < kt_end; ++kt) {
-          int const s = kt % kStages, use = kt / kStages;
-          if (!mbar_wait(&full_bar[s], use & 1, err, 3)) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          uint32_t const base = smem_u32(smem + s * kStageBytes);
-#pragma unroll
-          for (int ks = 0; ks < kTK / 16; ++ks) {
-#pragma unroll
-            for (int p = 0; p < kSlices; ++p) {
-#pragma unroll
-              for (int q = 0; q < kSlices; ++q) {
-                if (p + q >= kSlices) continue;  // 1-based p + q <= 7: 21 pairs
-                int const lvl = p + q;           // accumulator 0..5 (< kLevels)
-                uint64_t const ad = smem_desc(base + p * kABlk + ks * 256, 128, 512);
-                uint64_t const bd =
-                    smem_desc(base + kStageA + q * kBBlk + ks * 256, 128, 512);
-                uint32_t const acc = (started >> lvl) & 1u;
-                mma_bf16(tmem + static_cast<uint32_t>(lvl * kTN), ad, bd, acc);
-                started |= 1u << lvl;
-              }
-            }
-          }
-          mma_commit(&empty_bar[s]);  // stage s free once these MMAs complete
-        }
-        mma_commit(&acc_full);
-      }
-      mma_commit(&done_bar);
-      mbar_wait(&done_bar, 0, err, 4);
-    }
-  } else {
-    // Promotion warps 0-3: lane row = 32 * warp + lane of the M tile.
-    float hi[kTN], lo[kTN];
-#pragma unroll
-    for (int j = 0; j < kTN; ++j) hi[j] = lo[j] = 0.f;
-    uint32_t const lane_addr = tmem + (static_cast<uint32_t>(32 * warp) << 16);
-    for (int c = 0; c < n_chunks; ++c) {
-      if (!mbar_wait(&acc_full, c & 1, err, 5)) break;
-      tc_fence_after();
-#pragma unroll
-      for (int cb = 0; cb < kTN / 16; ++cb) {
-        // Chunk value sum_l E_l 2^-8l as a double-float (ch, cl): E_2 is exact,
-        // each further level enters through an error-free two-sum.
-        float ch[16], cl[16];
-        {
-          float v[16];
-          tmem_ld16(lane_addr + static_cast<uint32_t>(cb * 16), v);
-#pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            ch[u] = v[u];
-            cl[u] = 0.f;
-          }
-        }
-        for (int l = 1; l < kLevels; ++l) {
-          float const sc = __int_as_float((127 - 8 * l) << 23);  // 2^-8l
-          float v[16];
-          tmem_ld16(lane_addr + static_cast<uint32_t>(l * kTN + cb * 16), v);
-#pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            float s, e;
-            two_sum(ch[u], v[u] * sc, s, e);
-            ch[u] = s;
-            cl[u] += e;
-          }
-        }
-        // Running (hi, lo) += (ch, cl), renormalised so that |lo| <= ulp(hi)/2.
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          int const j = cb * 16 + u;
-          float s, e;
-          two_sum(hi[j], ch[u], s, e);
-          e += lo[j] + cl[u];
-          float const h = s + e;
-          lo[j] = e - (h - s);
-          hi[j] = h;
-        }
-      }
-      tc_fence_before();
-      mbar_arrive(&acc_empty);
-    }
-    // Result: D = (hi + lo) 2^(e_i + e_j - 14), rows (2i, 2i+1) = (Re, Im).
-    int const row = 32 * warp + lane;
-    int const i = mt * (kTM / 2) + row / 2;
-    if (i < g.nev) {
-      int const ei = expo[i];
-      double *outd = reinterpret_cast<double *>(
-          vdv + (static_cast<int64_t>(2 * ops[o]) * g.Lt + t) * g.nev * g.nev);
-#pragma unroll
-      for (int jj = 0; jj < kTN; ++jj) {
-        int const j = nt * kTN + jj;
-        if (j < g.nev) {
-          double const val = ldexp(static_cast<double>(hi[jj]) + static_cast<double>(lo[jj]),
-                                   ei + expo[j] - 14);
-          outd[2 * (i + static_cast<int64_t>(g.nev) * j) + (row & 1)] = val;
-        }
-      }
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(kTmemCols)
-                 : "memory");
-  }
+  uint8_t const *a_src = sbase + static_cast<int64_t>(mt) * k_tiles * kStageA;
+  uint8_t const *b_src =
+      sbase + b_off + (static_cast<int64_t>(o) * n_tiles + nt) * k_tiles * kStageB;
+  VdvEpilogue epi{reinterpret_cast<double *>(vdv + (static_cast<int64_t>(2 * ops[o]) * g.Lt + t) *
+                                                       g.nev * g.nev),
+                  reinterpret_cast<int32_t const *>(sbase + e_off), mt * (kTM / 2), nt * kTN,
+                  g.nev};
+  ozaki_tile(smem, a_src, b_src, k_tiles, err, epi);
 }
 
 }  // namespace
@@ -509,7 +170,7 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, double2 const *phase,
   uint8_t *base = static_cast<uint8_t *>(scratch);
   cudaError_t e = cudaFuncSetAttribute(ozaki_gemm_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(kStages * kStageBytes));
+                                       static_cast<int>(kSmemBytes));
   if (e != cudaSuccess) return e;
   // Padding rows of the last tiles stay zero: clear the slots once per call.
   e = cudaMemsetAsync(base, 0, L.slot_bytes * static_cast<size_t>(std::min<int64_t>(batch, nt)),
@@ -533,7 +194,7 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, double2 const *phase,
     ozaki_gemm_kernel<<<dim3(static_cast<unsigned>(L.m_tiles),
                              static_cast<unsigned>(L.n_tiles),
                              static_cast<unsigned>(n * nb)),
-                        192, kStages * kStageBytes, stream>>>(
+                        kThreads, kSmemBytes, stream>>>(
         base, L.slot_bytes, L.a_bytes, L.e_off, vdv, ops, n, static_cast<int32_t>(L.k_tiles),
         static_cast<int32_t>(L.n_tiles), tb, g, err);
     e = cudaGetLastError();

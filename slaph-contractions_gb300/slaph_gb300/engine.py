@@ -94,14 +94,15 @@ class Engine:
 
     def timings(self):
         """ms: VdaggerV, factors, products+traces, assembly, planning; launches;
-        the trace kernel alone (ms) and its launch count."""
-        out = np.zeros(8)
-        L.lib().slaph_engine_timings(self._h, L.dptr(out), 8)
+        per-entry trace kernel (ms, launches); trace GEMM (ms, launches);
+        operand slicing of the trace GEMM (ms)."""
+        out = np.zeros(12)
+        L.lib().slaph_engine_timings(self._h, L.dptr(out), 12)
         return out
 
     def stats(self):
-        out = np.zeros(6)
-        L.lib().slaph_engine_stats(self._h, L.dptr(out), 6)
+        out = np.zeros(8)
+        L.lib().slaph_engine_stats(self._h, L.dptr(out), 8)
         return out
 
 

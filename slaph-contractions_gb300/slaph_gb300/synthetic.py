@@ -167,3 +167,23 @@ CONFIGS["prof_16x32_pipi"] = Workload(
                     "C4cB:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1",
                     "C4cV:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1"]),
     seed=505, orthonormal=False, description="profiling case: 16^3x32 Nev=64 pipi")
+
+
+def grouped_pipi(name, nev, dilE, seed):
+    """The 32^3x64 operator and diagram set with momenta |p|^2 <= 1 on a 4^3x8
+    lattice.  Its trace lists contain dense groups (every A operand group with
+    every B group: 28 x 28 and 28 x 36) next to residual lists, so both trace
+    paths of the mixed precision mode run."""
+    return Workload(
+        name, Lt=8, L=4, nev=nev, n_rnd=5, dilT=4, dilE=dilE,
+        operators=[o.replace("p0,1,2,3,4", "p0,1") for o in PION_RHO_OPERATORS],
+        correlators=(["C2c:Q0:Op9:Q0:Op9:P0,1"]
+                     + [f"C3c:Q0:Op9:Q0:Op{k}:Q0:Op9:P0,1" for k in range(9)]
+                     + ["C4cD:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1",
+                        "C4cB:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1",
+                        "C4cV:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1"]),
+        seed=seed, description=f"pipi set, |p|^2 <= 1, 4^3x8, Nev {nev}, EI{dilE}")
+
+
+CONFIGS["pipi_groups_e4"] = grouped_pipi("pipi_groups_e4", nev=16, dilE=4, seed=606)
+CONFIGS["pipi_groups_e8"] = grouped_pipi("pipi_groups_e8", nev=32, dilE=8, seed=707)

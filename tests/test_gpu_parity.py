@@ -189,6 +189,34 @@ def test_vdaggerv_mixed_matches_fp64_and_contract(name, oracle_lib):
     assert e < REL_MIXED_CORR
 
 
+@pytest.mark.parametrize("name", ["pipi_groups_e4", "pipi_groups_e8"])
+def test_dense_trace_groups_match_oracle(name, oracle_lib):
+    """Trace lists forming dense groups: tensor-core GEMMs in the mixed mode,
+    the per-entry kernel in FP64; the residual lists take the per-entry
+    kernels in both.  Both accumulators, both precisions, against the oracle."""
+    from slaph_gb300 import synthetic
+    w = synthetic.CONFIGS[name]
+    gd, V, peram, noise = _synthetic_case(w)
+    eng = make_engine(gd, V, peram, noise)
+    vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
+    refs = {acc: oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, acc, -1,
+                                 gd.output_doubles()).reshape(-1, gd.dims.Lt)
+            for acc in (0, 1)}
+    eng.vdaggerv_build(0)
+    for acc in (0, 1):
+        assert rel_err(eng.contract(gd.plan_ptr, 0, acc), refs[acc]) < REL_FP64
+    eng.vdaggerv_build(1)
+    for acc in (0, 1):
+        out = eng.contract(gd.plan_ptr, 1, acc)
+        st, tim = eng.stats(), eng.timings()
+        assert 0 < st[7] < st[6], "both dense groups and residual lists must be present"
+        assert tim[9] > 0 and tim[7] > 0, "tensor-core and per-entry trace kernels must run"
+        e = rel_err(out, refs[acc])
+        print(f"{name}: mixed correlators (acc {acc}) max rel err {e:.2e}, "
+              f"{st[7] / st[6]:.0%} of trace entries in dense groups")
+        assert e < REL_MIXED_CORR
+
+
 def test_mixed_l4_goldens(l4):
     gd = l4["gd"]
     eng = make_engine(gd, l4["V"], l4["peram"], l4["noise"])
