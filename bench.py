@@ -223,9 +223,13 @@ def run_engine(args):
     # ---- end to end from host buffers
     barrier(dist)
     e2e0 = time.time()
+    e2e_parts = []
     for _ in range(args.steps):
+        t_a = time.time()
         upload()
+        t_b = time.time()
         step()
+        e2e_parts.append((t_b - t_a, time.time() - t_b))
     e2e = max_over_ranks(dist, (time.time() - e2e0) / args.steps)
     h2d = sum(v.nbytes for v in V) + sum(p.nbytes for p in peram) + noise.nbytes
     d2h = out.nbytes
@@ -307,7 +311,9 @@ def run_engine(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "host_buffers": "page-locked" if len(pinned) == len(V) + len(peram) + 1
-                else "pageable"},
+                else "pageable",
+                "upload_s": [round(a, 4) for a, _ in e2e_parts],
+                "step_s": [round(b, 4) for _, b in e2e_parts]},
         "gpu_launches": launches,
         "stages_ms": dict(zip(names, map(float, stage_ms))),
         "work": {"vdaggerv_tflop": vdv_flops / 1e12, "factor_tflop": stats[4] / 1e12,

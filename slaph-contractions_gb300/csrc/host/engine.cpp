@@ -129,6 +129,9 @@ void Engine::set_operators(slaph_vdv_op const *ops, int32_t n, int32_t index_of_
   phase_.reserve(sizeof(double2) * vol * std::max(n, 1));
   launch(dev::momenta(phase_.as<double2>(), mom_dev_.as<int32_t>(), n, geo_, stream_),
          "momenta");
+  phase_fx_.reserve(sizeof(longlong2) * vol * std::max(n, 1));
+  launch(dev::phase_fixed(phase_fx_.as<longlong2>(), phase_.as<double2>(), vol * n, stream_),
+         "phase_fixed");
   vdv_.reserve(sizeof(double2) * 2LL * std::max(n, 1) * dims_.Lt * dims_.nev * dims_.nev);
   SLAPH_CK(cudaStreamSynchronize(stream_));
   ops_set_ = true;
@@ -181,7 +184,7 @@ void Engine::vdaggerv_build(int precision) {
   }
   SLAPH_CK(cudaEventRecord(ev_[0], stream_));
   if (precision == SLAPH_MIXED) {
-    launch(dev::vdaggerv_tc(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
+    launch(dev::vdaggerv_tc(vdv_.as<double2>(), V_.as<double2>(), phase_fx_.as<longlong2>(),
                             list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_,
                             tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_),
            "vdaggerv_tc");

@@ -87,7 +87,7 @@ class Engine {
   cudaEvent_t ev_[8] = {};
   std::vector<cudaEvent_t> tc_ev_;  // three per tensor-core trace batch
 
-  DevBuf V_, peram_, noise_, phase_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
+  DevBuf V_, peram_, noise_, phase_, phase_fx_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
   std::vector<slaph_vdv_op> ops_;
   int32_t index_of_unity_ = -1;
   bool ops_set_ = false, vdv_built_ = false;

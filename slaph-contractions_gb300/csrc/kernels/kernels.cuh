@@ -72,8 +72,12 @@ cudaError_t vdaggerv_fp64(double2 *vdv, double2 const *V, double2 const *phase,
 // processed per launch (vdaggerv_tc_batch picks it from the SM count and a
 // memory cap); err: device int, set non-zero when a bounded wait gave up.
 size_t vdaggerv_tc_scratch_bytes(Geometry g, int32_t n_ops, int32_t batch);
+// phase_fx[k] = round(phase[k] 2^62) per component, the fixed-point phases the
+// split-precision VdaggerV multiplies with integer arithmetic.
+cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
+                        cudaStream_t stream);
 int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes);
-cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, double2 const *phase,
+cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_fx,
                         int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream);
 // Identity blocks for code 2*op (and 2*op+1).

@@ -202,13 +202,46 @@ __device__ __forceinline__ void slice6(long long F, uint16_t (&out)[kSlices]) {
   }
 }
 
-// Writes the slices of complex element x (K index m, K' = 2m, 2m+1) of A row
-// `row` of a tile stream laid out [m_tile][k_tile][slice][kTM x kTK]: row 2r
-// gets (Re x, Im x), row 2r+1 gets (-Im x, Re x).
-__device__ __forceinline__ void put_a(uint8_t *region, int64_t k_tiles, int row, int64_t m,
-                                      double2 x, int e) {
+// The same for a float, with integer operations only: round(v 2^(55-e)) for
+// |v| < 2^e (then the shift below is at most 31 and |F| < 2^55).
+__device__ __forceinline__ long long fixed55f(float v, int e) {
+  int const bits = __float_as_int(v);
+  int const ex = (bits >> 23) & 0xFF;
+  if (ex == 0) return 0;  // zero or subnormal: below 2^-126 2^e, negligible here
+  long long const m = (bits & 0x7FFFFF) | 0x800000;  // v = m 2^(ex - 150)
+  int const sh = ex - 150 + 55 - e;
+  long long F;
+  if (sh >= 0) {
+    F = m << (sh < 31 ? sh : 31);
+  } else if (sh > -40) {
+    F = (m + (1LL << (-sh - 1))) >> (-sh);
+  } else {
+    F = 0;
+  }
+  return bits < 0 ? -F : F;
+}
+
+// Exponent e with max |x| < 2^e, from the largest |x| given as the bit
+// pattern of a float (0 for a zero maximum).
+__device__ __forceinline__ int expo_of_absbits(unsigned int b) {
+  if (b == 0) return 0;
+  int const ex = static_cast<int>(b >> 23);
+  return ex == 0 ? -125 : ex - 126;
+}
+// The same for a double bit pattern.
+__device__ __forceinline__ int expo_of_absbits64(unsigned long long b) {
+  if (b == 0) return 0;
+  int const ex = static_cast<int>(b >> 52);
+  return ex == 0 ? -1021 : ex - 1022;
+}
+
+// Writes the slices of complex element x = (fr, fi) 2^(e-55) (K index m,
+// K' = 2m, 2m+1) of A row `row` of a tile stream laid out
+// [m_tile][k_tile][slice][kTM x kTK]: row 2r gets (Re x, Im x), row 2r+1 gets
+// (-Im x, Re x).
+__device__ __forceinline__ void put_a_fx(uint8_t *region, int64_t k_tiles, int row, int64_t m,
+                                         long long fr, long long fi) {
   uint16_t sre[kSlices], sim[kSlices], snim[kSlices];
-  long long const fr = fixed55(x.x, e), fi = fixed55(x.y, e);
   slice6(fr, sre);
   slice6(fi, sim);
   slice6(-fi, snim);
@@ -228,11 +261,11 @@ __device__ __forceinline__ void put_a(uint8_t *region, int64_t k_tiles, int row,
 
 // The same for B column `col` of a stream laid out [n_tile][k_tile][slice][kTN x kTK]:
 // (Re y, Im y).
-__device__ __forceinline__ void put_b(uint8_t *region, int64_t k_tiles, int col, int64_t m,
-                                      double2 y, int e) {
+__device__ __forceinline__ void put_b_fx(uint8_t *region, int64_t k_tiles, int col, int64_t m,
+                                         long long fr, long long fi) {
   uint16_t sre[kSlices], sim[kSlices];
-  slice6(fixed55(y.x, e), sre);
-  slice6(fixed55(y.y, e), sim);
+  slice6(fr, sre);
+  slice6(fi, sim);
   int const nt = col / kTN, r = col % kTN;
   int64_t const kt = m / (kTK / 2);
   int const k = 2 * static_cast<int>(m % (kTK / 2));
@@ -241,6 +274,15 @@ __device__ __forceinline__ void put_b(uint8_t *region, int64_t k_tiles, int col,
   for (int p = 0; p < kSlices; ++p)
     *reinterpret_cast<uint32_t *>(blk + p * kBBlk + core_off(r, k)) =
         static_cast<uint32_t>(sre[p]) | (static_cast<uint32_t>(sim[p]) << 16);
+}
+
+__device__ __forceinline__ void put_a(uint8_t *region, int64_t k_tiles, int row, int64_t m,
+                                      double2 x, int e) {
+  put_a_fx(region, k_tiles, row, m, fixed55(x.x, e), fixed55(x.y, e));
+}
+__device__ __forceinline__ void put_b(uint8_t *region, int64_t k_tiles, int col, int64_t m,
+                                      double2 y, int e) {
+  put_b_fx(region, k_tiles, col, m, fixed55(y.x, e), fixed55(y.y, e));
 }
 
 // Exponent e with max |x| < 2^e for a positive maximum (0 for m == 0).

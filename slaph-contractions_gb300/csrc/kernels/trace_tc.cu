@@ -32,7 +32,9 @@ using namespace tc;
 
 constexpr int kSliceThreads = 128;
 
-// One matrix per CTA: exponent of its largest |re|, |im|, then its slices.
+// One matrix per CTA: exponent of its largest |re|, |im| (from the high
+// words), then its slices.  Integer and FP32 operations only: the fixed-point
+// value of a double-float entry is the sum of those of its two words.
 template <bool kIsA>
 __global__ void __launch_bounds__(kSliceThreads)
     trace_slice_kernel(uint8_t *scratch, int32_t *expo, TrSlice const *items,
@@ -41,32 +43,30 @@ __global__ void __launch_bounds__(kSliceThreads)
   int64_t const ms = static_cast<int64_t>(eds) * eds;
   int64_t const k_tiles = ms / (kTK / 2);
   float4 const *src = slots + static_cast<int64_t>(it.slot) * ms;
-  double mx = 0;
+  unsigned int mx = 0;
   for (int64_t m = threadIdx.x; m < ms; m += kSliceThreads) {
     float4 const v = src[m];
-    double const re = static_cast<double>(v.x) + static_cast<double>(v.y);
-    double const im = static_cast<double>(v.z) + static_cast<double>(v.w);
-    mx = fmax(mx, fmax(fabs(re), fabs(im)));
+    mx = max(mx, max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.z) & 0x7FFFFFFFu));
   }
-#pragma unroll
-  for (int s = 16; s > 0; s >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, s));
-  __shared__ double red[kSliceThreads / 32];
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  __shared__ unsigned int red[kSliceThreads / 32];
   if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = mx;
   __syncthreads();
   mx = red[0];
 #pragma unroll
-  for (int w = 1; w < kSliceThreads / 32; ++w) mx = fmax(mx, red[w]);
-  int const e = expo_of_max(mx);
+  for (int w = 1; w < kSliceThreads / 32; ++w) mx = max(mx, red[w]);
+  // |hi + lo| < 2^e whenever |hi| < 2^e (|lo| <= ulp(hi) / 2).
+  int const e = expo_of_absbits(mx);
   if (threadIdx.x == 0) expo[it.expo] = e;
   uint8_t *region = scratch + it.dst;
   for (int64_t m = threadIdx.x; m < ms; m += kSliceThreads) {
     float4 const v = src[m];
-    double const re = static_cast<double>(v.x) + static_cast<double>(v.y);
-    double const im = static_cast<double>(v.z) + static_cast<double>(v.w);
+    long long const fr = fixed55f(v.x, e) + fixed55f(v.y, e);
+    long long const fi = fixed55f(v.z, e) + fixed55f(v.w, e);
     if (kIsA)
-      put_a(region, k_tiles, it.row, m, make_double2(re, -im), e);
+      put_a_fx(region, k_tiles, it.row, m, fr, -fi);  // conj: A' rows give sum x_k y_k
     else
-      put_b(region, k_tiles, it.row, m, make_double2(re, im), e);
+      put_b_fx(region, k_tiles, it.row, m, fr, fi);
   }
 }
 

@@ -62,22 +62,35 @@ __global__ void slice_a_kernel(uint16_t *out, double2 const *Vt, int32_t const *
 }
 
 // B slices of W = diag(phase_op) V: [op][n_tile][k_tile][slice][kTN x kTK].
-__global__ void slice_b_kernel(uint16_t *out, double2 const *Vt, double2 const *phase,
+// The phase product is taken in fixed point with integer operations only:
+// with V = F_v 2^(e-55) and phase = P 2^-62 (|P| <= 2^62),
+// W = ((F_v 4) P / 2^64) 2^(e-55), the high word of a 128-bit product.
+__global__ void slice_b_kernel(uint16_t *out, double2 const *Vt, longlong2 const *phase_fx,
                                int32_t const *ops, int32_t const *expo, int32_t k_tiles,
                                int32_t n_tiles, Geometry g) {
   int64_t const x = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   int const j = blockIdx.y;
   int const o = blockIdx.z;
   if (x >= static_cast<int64_t>(k_tiles) * (kTK / 2)) return;
-  double2 w = make_double2(0, 0);
+  int const e = expo[j];
+  long long wr = 0, wi = 0;
   if (x < g.dim_row) {
     double2 const v = Vt[static_cast<int64_t>(j) * g.dim_row + x];
-    double2 const ph = phase[static_cast<int64_t>(ops[o]) * (g.dim_row / 3) + x / 3];
-    w = make_double2(ph.x * v.x - ph.y * v.y, ph.x * v.y + ph.y * v.x);
+    longlong2 const ph = phase_fx[static_cast<int64_t>(ops[o]) * (g.dim_row / 3) + x / 3];
+    long long const vr = fixed55(v.x, e) * 4, vi = fixed55(v.y, e) * 4;
+    wr = __mul64hi(vr, ph.x) - __mul64hi(vi, ph.y);
+    wi = __mul64hi(vr, ph.y) + __mul64hi(vi, ph.x);
   }
   uint8_t *region = reinterpret_cast<uint8_t *>(out) +
                     static_cast<int64_t>(o) * n_tiles * k_tiles * kStageB;
-  put_b(region, k_tiles, j, x, w, expo[j]);
+  put_b_fx(region, k_tiles, j, x, wr, wi);
+}
+
+__global__ void phase_fixed_kernel(longlong2 *dst, double2 const *src, int64_t n) {
+  int64_t const k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  double2 const v = src[k];
+  dst[k] = make_longlong2(__double2ll_rn(ldexp(v.x, 62)), __double2ll_rn(ldexp(v.y, 62)));
 }
 
 // Epilogue of one VdaggerV tile: D = (hi + lo) 2^(e_i + e_j - 14), rows
@@ -159,7 +172,15 @@ int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t ma
   return static_cast<int32_t>(want < 1 ? 1 : want);
 }
 
-cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, double2 const *phase,
+cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
+                        cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  phase_fixed_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(phase_fx,
+                                                                              phase, n);
+  return cudaGetLastError();
+}
+
+cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_fx,
                         int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream) {
   if (n == 0 || nt == 0) return cudaSuccess;
@@ -188,7 +209,7 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, double2 const *phase,
       slice_a_kernel<<<dim3(xb, g.nev), 256, 0, stream>>>(
           reinterpret_cast<uint16_t *>(slot), Vt, expo, static_cast<int32_t>(L.k_tiles), g);
       slice_b_kernel<<<dim3(xb, g.nev, n), 256, 0, stream>>>(
-          reinterpret_cast<uint16_t *>(slot + L.a_bytes), Vt, phase, ops, expo,
+          reinterpret_cast<uint16_t *>(slot + L.a_bytes), Vt, phase_fx, ops, expo,
           static_cast<int32_t>(L.k_tiles), static_cast<int32_t>(L.n_tiles), g);
     }
     ozaki_gemm_kernel<<<dim3(static_cast<unsigned>(L.m_tiles),
