@@ -157,42 +157,49 @@ def run_engine(args):
     w = synthetic.CONFIGS[args.workload]
     gd = GlobalData.from_infile(w.write_infile())
     dims = gd.dims
+    # Inputs in driver-pinned host memory (slaph_host_alloc), as a production
+    # driver holds the buffers it uploads every configuration.
+    from slaph_gb300.engine import pinned_empty
+
+    def pinned_copy(a):
+        p = pinned_empty(a.shape, a.dtype)
+        p[...] = a
+        return p
+
     t_gen = time.time()
-    V = [w.eigenvectors(t) for t in range(w.Lt)]
-    peram = [np.ascontiguousarray(w.perambulator(r)) for r in range(w.n_rnd)]
-    noise = np.ascontiguousarray(np.stack([w.noise(r) for r in range(w.n_rnd)]))
+    V = [pinned_copy(w.eigenvectors(t)) for t in range(w.Lt)]
+    peram = [pinned_copy(w.perambulator(r)) for r in range(w.n_rnd)]
+    noise = pinned_copy(np.stack([w.noise(r) for r in range(w.n_rnd)]))
     t_gen = time.time() - t_gen
     precision = 1 if args.precision == "mixed" else 0
 
     eng = Engine(dims)
     eng.set_operators(gd.plan)
 
+    upload_calls = {"eigenvectors": [], "perambulators": [], "noise": []}
+
     def upload():
         for t, v in enumerate(V):
+            t0 = time.perf_counter()
             eng.set_eigenvectors(t, v)
+            upload_calls["eigenvectors"].append(time.perf_counter() - t0)
         for r, p in enumerate(peram):
+            t0 = time.perf_counter()
             eng.set_perambulator(r, p)
+            upload_calls["perambulators"].append(time.perf_counter() - t0)
         for r in range(noise.shape[0]):
+            t0 = time.perf_counter()
             eng.set_random_vector(r, noise[r])
+            upload_calls["noise"].append(time.perf_counter() - t0)
 
     def step():
         eng.vdaggerv_build(precision)
         out = eng.contract(gd.plan_ptr, precision, 0, args.single_block_pair)
         return out
 
-    # Page-locked host inputs, as a production driver would hold them.
-    t_pin = time.time()
-    pinned = []
-    try:
-        for a in [*V, *peram, noise]:
-            Engine.pin(a)
-            pinned.append(a)
-    except Exception as e:  # keep going with pageable buffers, and say so
-        print(f"bench: host_register failed ({e}); end-to-end copies are pageable",
-              file=sys.stderr)
-    t_pin = time.time() - t_pin
 
     upload()
+    first_upload = {k: round(1e3 * sum(v), 1) for k, v in upload_calls.items()}
     t0 = time.time()
     out = step()  # also builds and uploads the (config-independent) schedule
     first = time.time() - t0
@@ -222,6 +229,8 @@ def run_engine(args):
 
     # ---- end to end from host buffers
     barrier(dist)
+    for v in upload_calls.values():
+        v.clear()
     e2e0 = time.time()
     e2e_parts = []
     for _ in range(args.steps):
@@ -310,9 +319,14 @@ def run_engine(args):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "host_buffers": "page-locked" if len(pinned) == len(V) + len(peram) + 1
-                else "pageable",
+                "host_buffers": "page-locked (slaph_host_alloc)",
                 "upload_s": [round(a, 4) for a, _ in e2e_parts],
+                "upload_call_ms": {k: [round(1e3 * min(v), 3), round(1e3 * float(np.median(v)), 3),
+                                       round(1e3 * max(v), 3), round(1e3 * sum(v), 1)]
+                                   for k, v in upload_calls.items() if v},
+                "first_upload_ms": first_upload,
+                "slow_eigenvector_calls": [(i % w.Lt, round(1e3 * x, 1)) for i, x in
+                                           enumerate(upload_calls["eigenvectors"]) if x > 0.01],
                 "step_s": [round(b, 4) for _, b in e2e_parts]},
         "gpu_launches": launches,
         "stages_ms": dict(zip(names, map(float, stage_ms))),
@@ -320,7 +334,7 @@ def run_engine(args):
                  "product_trace_tflop": stats[5] / 1e12, "factors": stats[0],
                  "products": stats[1], "trace_entries": stats[2], "terms": stats[3]},
         "planning_s": plan_s, "first_step_s": first, "input_generation_s": t_gen,
-        "host_register_s": t_pin,
+
         "roofline": roofline, "roofline_others": others, "kernels_ms": kernels_ms,
         "clocks": clocks,
         "wall_s_per_step": wall / args.steps,

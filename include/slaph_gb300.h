@@ -224,10 +224,17 @@ int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V)
 int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram);
 int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise);
 
-/* Page-locks (and unlocks) a caller-owned host buffer so that the set_*
- * copies above run at the full host-device link rate instead of through a
- * staging copy.  No counterpart in the reference (its inputs never leave host
- * memory).  Registration outlives engines; unregister before freeing. */
+/* Page-locked host memory for the inputs, so that the set_* copies above run
+ * at the full host-device link rate.  slaph_host_alloc returns driver-pinned
+ * memory (cudaHostAlloc) that keeps that rate for its whole lifetime; free it
+ * with slaph_host_free.  slaph_host_register / _unregister instead register a
+ * caller-owned buffer; on systems whose GPU reads host page tables (Grace),
+ * pages the kernel later moves (e.g. huge-page collapse of large anonymous
+ * mappings) fall back to a slow staged copy, so long-lived input buffers are
+ * better taken from slaph_host_alloc.  No counterpart in the reference (its
+ * inputs never leave host memory). */
+int slaph_host_alloc(size_t bytes, void **out);
+int slaph_host_free(void *ptr);
 int slaph_host_register(void *ptr, size_t bytes);
 int slaph_host_unregister(void *ptr);
 

@@ -1,5 +1,6 @@
 // C ABI of the engine (include/slaph_gb300.h).
 #include <memory>
+#include <string>
 
 #include "capi_util.hpp"
 #include "engine.hpp"
@@ -47,6 +48,27 @@ int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const doubl
 
 int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise) {
   return slaph::guarded([&] { get(eng).set_random_vector(rnd_id, noise); });
+}
+
+int slaph_host_alloc(size_t bytes, void **out) {
+  return slaph::guarded([&] {
+    if (!out || bytes == 0) throw slaph::ArgError("null output or empty size");
+    *out = nullptr;
+    cudaError_t const e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+      *out = nullptr;
+      (void)cudaGetLastError();
+      throw slaph::NoMemError(std::string("cudaHostAlloc of ") + std::to_string(bytes) +
+                              " bytes failed: " + cudaGetErrorString(e));
+    }
+  });
+}
+
+int slaph_host_free(void *ptr) {
+  return slaph::guarded([&] {
+    if (!ptr) throw slaph::ArgError("null host buffer");
+    slaph::cuda_check(cudaFreeHost(ptr), "cudaFreeHost");
+  });
 }
 
 int slaph_host_register(void *ptr, size_t bytes) {

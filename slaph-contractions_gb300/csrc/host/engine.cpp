@@ -2,6 +2,8 @@
 #include "engine.hpp"
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cstring>
 #include <numeric>
 
@@ -93,6 +95,7 @@ Engine::Engine(slaph_dims const &d) : dims_(d) {
   SLAPH_CK(cudaMemsetAsync(noise_.as<void>(), 0, noise_.size(), stream_));
   SLAPH_CK(cudaMemsetAsync(peram_.as<void>(), 0, peram_.size(), stream_));
   SLAPH_CK(dev::upload_gamma(stream_));
+  SLAPH_CK(dev::upload_gamma_tc(stream_));
   SLAPH_CK(cudaStreamSynchronize(stream_));
 }
 
@@ -415,6 +418,400 @@ void Engine::prepare_trace_tc(DeviceSchedule &ds) {
   ds.tc_ready = true;
 }
 
+// Tensor-core plan of the Q1/Q2 factors (factor_tc.cu).  Per timeslice t:
+//   X1[t]  rows (Q1R r at t, a), columns (r2, b, d, c), K = v:
+//          A = conj(Q1R_r(a, v)), B = P_r2((4t+d) nev + v, b eds + c)
+//   Q2M[t] rows (pair (b1, r1), a, bd), columns (VdaggerV code, v), K = w:
+//          A = P_r1((4t+bd) nev + w, b1 eds + a) (conjugated by the GEMM form),
+//          B = VdV_code(t)(w, v)
+//   Q2     per complete bipartite set of (Q2M instance m) x (gamma, r2, b2):
+//          rows (m, a), columns (gamma, r2, b2, c), K = (bd, v):
+//          A = conj(s(bd, a) Q2M_m(a, bd nev + v)),
+//          B = Gval[gamma][bd] P_r2((4t+Grow[gamma][bd]) nev + v, b2 eds + c)
+// Dense FP64 outputs go to f_out_; gathers write the factor slots.
+void Engine::prepare_factor_tc(DeviceSchedule &ds) {
+  if (ds.f_ready) return;
+  Schedule const &s = ds.s;
+  int32_t const eds = s.eds, nev = dims_.nev, dilE = dims_.dilE, nb = geo_.nb;
+  int32_t const n_rnd = dims_.n_rnd, Lt = dims_.Lt;
+  int64_t const prow = 4LL * nev * Lt;            // perambulator rows
+  int64_t const prs = prow * nb * eds;            // perambulator elements per random vector
+  int64_t const blk = static_cast<int64_t>(nev) * nev;
+  int32_t const kt1 = dev::gemm_k_tiles(nev), kt2 = dev::gemm_k_tiles(4LL * nev);
+  size_t const a_tile1 = dev::tc_a_bytes(1, kt1), b_tile1 = dev::tc_b_bytes(1, kt1);
+  size_t const a_tile2 = dev::tc_a_bytes(1, kt2), b_tile2 = dev::tc_b_bytes(1, kt2);
+  size_t const cap = std::max(tc_scratch_.size(), kTraceScratchMin);
+  int64_t const out_cap = int64_t{1} << 29;  // double2 per batch (8 GiB)
+
+  // Instances per timeslice.
+  std::vector<std::vector<int32_t>> q1r_t(Lt), q2m_t(Lt), q1_t(Lt), q2_t(Lt);
+  for (size_t i = 0; i < s.q1r.size(); ++i) q1r_t[s.q1r[i].t].push_back(static_cast<int32_t>(i));
+  for (size_t i = 0; i < s.q2m.size(); ++i) q2m_t[s.q2m[i].t].push_back(static_cast<int32_t>(i));
+  for (size_t i = 0; i < s.q1.size(); ++i) q1_t[s.q1[i].t].push_back(static_cast<int32_t>(i));
+  for (size_t i = 0; i < s.q2.size(); ++i) q2_t[s.q2[i].t].push_back(static_cast<int32_t>(i));
+
+  std::vector<dev::GVec> vec;
+  std::vector<dev::TrTile> tiles;
+  std::vector<dev::Q1Gather> g1;
+  std::vector<dev::Q2Gather> g2;
+  ds.f_batches.clear();
+  size_t need = 0;
+  int64_t need_out = 0, need_expo = 0;
+
+  auto add_vec = [&](int64_t dst, int32_t row, int32_t expo, int64_t stride, int32_t seg_len,
+                     std::initializer_list<dev::GSeg> segs) {
+    dev::GVec v{};
+    v.dst = dst;
+    v.stride = stride;
+    v.row = row;
+    v.expo = expo;
+    v.n_seg = static_cast<int32_t>(segs.size());
+    v.seg_len = seg_len;
+    int k = 0;
+    for (auto const &g : segs) v.seg[k++] = g;
+    vec.push_back(v);
+  };
+  auto add_tiles = [&](int64_t a_reg, int64_t b_reg, size_t a_tile, size_t b_tile, int32_t rows,
+                       int32_t cols, int64_t out, int32_t ea, int32_t eb) {
+    int32_t const mts = (rows + dev::kTrTileRows - 1) / dev::kTrTileRows;
+    int32_t const nts = (cols + dev::kTrTileCols - 1) / dev::kTrTileCols;
+    for (int32_t mt = 0; mt < mts; ++mt)
+      for (int32_t nt = 0; nt < nts; ++nt) {
+        dev::TrTile t{};
+        t.a_src = a_reg + static_cast<int64_t>(mt) * static_cast<int64_t>(a_tile);
+        t.b_src = b_reg + static_cast<int64_t>(nt) * static_cast<int64_t>(b_tile);
+        t.out = out + static_cast<int64_t>(nt) * dev::kTrTileCols * rows +
+                static_cast<int64_t>(mt) * dev::kTrTileRows;
+        t.ea = ea + mt * dev::kTrTileRows;
+        t.eb = eb + nt * dev::kTrTileCols;
+        t.rows = std::min(dev::kTrTileRows, rows - mt * dev::kTrTileRows);
+        t.cols = std::min(dev::kTrTileCols, cols - nt * dev::kTrTileCols);
+        t.ld = rows;
+        tiles.push_back(t);
+      }
+  };
+
+  // Per-timeslice pieces, appended to the current batch until a cap is hit.
+  struct TPlan {
+    size_t s1 = 0, s2 = 0;  // scratch bytes of phase 1 / 2
+    int64_t out = 0;        // dense output doubles2
+  };
+  auto t_sizes = [&](int t, std::vector<std::vector<int32_t>> &bic_rows,
+                     std::vector<std::vector<std::array<int32_t, 3>>> &bic_cols) {
+    TPlan p;
+    int32_t const nr = static_cast<int32_t>(q1r_t[t].size());
+    int32_t const x1_rows = nr * eds, x1_cols = n_rnd * nb * 4 * eds;
+    std::map<std::pair<int32_t, int32_t>, int32_t> pairs;
+    std::map<int32_t, int32_t> codes;
+    for (int32_t m : q2m_t[t]) {
+      pairs.emplace(std::make_pair(s.q2m[m].b1, s.q2m[m].r1), 0);
+      codes.emplace(s.q2m[m].vdv, 0);
+    }
+    int32_t const q2m_rows = static_cast<int32_t>(pairs.size()) * eds * 4;
+    int32_t const q2m_cols = static_cast<int32_t>(codes.size()) * nev;
+    if (nr > 0)
+      p.s1 += dev::tc_a_bytes(x1_rows, kt1) + dev::tc_b_bytes(x1_cols, kt1);
+    if (!q2m_t[t].empty())
+      p.s1 += dev::tc_a_bytes(q2m_rows, kt1) + dev::tc_b_bytes(q2m_cols, kt1);
+    p.out += static_cast<int64_t>(x1_rows) * x1_cols + static_cast<int64_t>(q2m_rows) * q2m_cols;
+    // Q2 bicliques: Q2M instances with equal sets of (gamma, r2, b2).
+    std::map<int32_t, std::vector<std::array<int32_t, 3>>> cols_of;
+    for (int32_t q : q2_t[t]) cols_of[s.q2[q].m].push_back({s.q2[q].gamma, s.q2[q].r2, s.q2[q].b2});
+    std::map<std::vector<std::array<int32_t, 3>>, std::vector<int32_t>> groups;
+    for (auto &kv : cols_of) {
+      auto v = kv.second;
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      groups[v].push_back(kv.first);
+    }
+    bic_rows.clear();
+    bic_cols.clear();
+    for (auto &kv : groups) {
+      bic_rows.push_back(kv.second);
+      bic_cols.push_back(kv.first);
+      int32_t const rows = static_cast<int32_t>(kv.second.size()) * eds;
+      int32_t const cols = static_cast<int32_t>(kv.first.size()) * eds;
+      p.s2 += dev::tc_a_bytes(rows, kt2) + dev::tc_b_bytes(cols, kt2);
+      p.out += static_cast<int64_t>(rows) * cols;
+    }
+    return p;
+  };
+
+  size_t used1 = 0, used2 = 0;
+  int64_t used_out = 0;
+  int32_t expo = 0;
+  std::vector<int> batch_ts;
+  auto flush = [&](void) {
+    if (batch_ts.empty()) return;
+    // Phase 1 then phase 2 items of every timeslice of the batch.
+    DeviceSchedule::FBatch b{};
+    int64_t out = 0;
+    size_t off1 = 0, off2 = 0;
+    expo = 0;
+    struct TOut {
+      int64_t x1, q2m;
+      int32_t x1_rows, q2m_rows;
+      std::map<std::pair<int32_t, int32_t>, int32_t> pairs;
+      std::map<int32_t, int32_t> codes;
+      std::vector<std::vector<int32_t>> bic_rows;
+      std::vector<std::vector<std::array<int32_t, 3>>> bic_cols;
+      std::map<int32_t, int32_t> rloc;
+    };
+    std::vector<TOut> tos(batch_ts.size());
+    // -- phase 1 vectors: X1 A (df source), Q2M A (f64), X1 B (f64), Q2M B (f64)
+    auto begin = [&](int64_t (&r)[2]) { r[0] = static_cast<int64_t>(vec.size()); };
+    auto end = [&](int64_t (&r)[2]) { r[1] = static_cast<int64_t>(vec.size()) - r[0]; };
+    std::vector<int64_t> regA_x1(batch_ts.size()), regB_x1(batch_ts.size()),
+        regA_q2m(batch_ts.size()), regB_q2m(batch_ts.size());
+    std::vector<int32_t> eA_x1(batch_ts.size()), eB_x1(batch_ts.size()),
+        eA_q2m(batch_ts.size()), eB_q2m(batch_ts.size());
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      int const t = batch_ts[k];
+      TOut &o = tos[k];
+      for (int32_t r : q1r_t[t]) o.rloc.emplace(r, static_cast<int32_t>(o.rloc.size()));
+      for (int32_t m : q2m_t[t]) {
+        o.pairs.emplace(std::make_pair(s.q2m[m].b1, s.q2m[m].r1), 0);
+        o.codes.emplace(s.q2m[m].vdv, 0);
+      }
+      int32_t i = 0;
+      for (auto &kv : o.pairs) kv.second = i++;
+      i = 0;
+      for (auto &kv : o.codes) kv.second = i++;
+      o.x1_rows = static_cast<int32_t>(o.rloc.size()) * eds;
+      o.q2m_rows = static_cast<int32_t>(o.pairs.size()) * eds * 4;
+      o.x1 = out;
+      out += static_cast<int64_t>(o.x1_rows) * n_rnd * nb * 4 * eds;
+      o.q2m = out;
+      out += static_cast<int64_t>(o.q2m_rows) * static_cast<int64_t>(o.codes.size()) * nev;
+    }
+    begin(b.a_x1);
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      TOut &o = tos[k];
+      regA_x1[k] = static_cast<int64_t>(off1);
+      eA_x1[k] = expo;
+      for (auto const &kv : o.rloc)
+        for (int32_t a = 0; a < eds; ++a)
+          add_vec(regA_x1[k], kv.second * eds + a, expo++, eds, nev,
+                  {{static_cast<int64_t>(kv.first) * nev * eds + a, 0, 0}});
+      off1 += dev::tc_a_bytes(std::max(o.x1_rows, 1), kt1);
+    }
+    end(b.a_x1);
+    begin(b.a_q2m);
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      int const t = batch_ts[k];
+      TOut &o = tos[k];
+      regA_q2m[k] = static_cast<int64_t>(off1);
+      eA_q2m[k] = expo;
+      for (auto const &kv : o.pairs) {
+        int32_t const b1 = kv.first.first, r1 = kv.first.second, p = kv.second;
+        for (int32_t a = 0; a < eds; ++a)
+          for (int32_t bd = 0; bd < 4; ++bd)
+            add_vec(regA_q2m[k], (p * eds + a) * 4 + bd, eA_q2m[k] + (p * eds + a) * 4 + bd, 1,
+                    nev,
+                    {{r1 * prs + (4LL * t + bd) * nev + prow * (static_cast<int64_t>(b1) * eds + a),
+                      0, 0}});
+      }
+      expo += o.q2m_rows;
+      off1 += dev::tc_a_bytes(std::max(o.q2m_rows, 1), kt1);
+    }
+    end(b.a_q2m);
+    begin(b.b_x1);
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      int const t = batch_ts[k];
+      regB_x1[k] = static_cast<int64_t>(off1);
+      eB_x1[k] = expo;
+      int32_t const cols = n_rnd * nb * 4 * eds;
+      if (tos[k].x1_rows > 0) {
+        for (int32_t r2 = 0; r2 < n_rnd; ++r2)
+          for (int32_t b2 = 0; b2 < nb; ++b2)
+            for (int32_t d = 0; d < 4; ++d)
+              for (int32_t c = 0; c < eds; ++c)
+                add_vec(regB_x1[k], ((r2 * nb + b2) * 4 + d) * eds + c, expo++, 1, nev,
+                        {{r2 * prs + (4LL * t + d) * nev + prow * (static_cast<int64_t>(b2) * eds + c),
+                          0, 0}});
+        off1 += dev::tc_b_bytes(cols, kt1);
+      }
+    }
+    end(b.b_x1);
+    begin(b.b_q2m);
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      int const t = batch_ts[k];
+      TOut &o = tos[k];
+      regB_q2m[k] = static_cast<int64_t>(off1);
+      eB_q2m[k] = expo;
+      for (auto const &kv : o.codes)
+        for (int32_t v = 0; v < nev; ++v)
+          add_vec(regB_q2m[k], kv.second * nev + v, expo++, 1, nev,
+                  {{(static_cast<int64_t>(kv.first) * Lt + t) * blk + static_cast<int64_t>(nev) * v,
+                    0, 0}});
+      if (!o.codes.empty())
+        off1 += dev::tc_b_bytes(static_cast<int32_t>(o.codes.size()) * nev, kt1);
+    }
+    end(b.b_q2m);
+    b.t1[0] = static_cast<int64_t>(tiles.size());
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      TOut &o = tos[k];
+      if (o.x1_rows > 0)
+        add_tiles(regA_x1[k], regB_x1[k], a_tile1, b_tile1, o.x1_rows, n_rnd * nb * 4 * eds, o.x1,
+                  eA_x1[k], eB_x1[k]);
+      if (o.q2m_rows > 0)
+        add_tiles(regA_q2m[k], regB_q2m[k], a_tile1, b_tile1, o.q2m_rows,
+                  static_cast<int32_t>(o.codes.size()) * nev, o.q2m, eA_q2m[k], eB_q2m[k]);
+    }
+    b.t1[1] = static_cast<int64_t>(tiles.size()) - b.t1[0];
+    need = std::max(need, off1);
+    // -- phase 2: Q2 bicliques (A from the Q2M outputs, B from the perambulators)
+    std::vector<std::vector<int64_t>> regA2(batch_ts.size()), regB2(batch_ts.size()),
+        out2(batch_ts.size());
+    std::vector<std::vector<int32_t>> eA2(batch_ts.size()), eB2(batch_ts.size());
+    for (size_t k = 0; k < batch_ts.size(); ++k) t_sizes(batch_ts[k], tos[k].bic_rows, tos[k].bic_cols);
+    begin(b.a_q2);
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      TOut &o = tos[k];
+      int64_t const ld = o.q2m_rows;
+      for (size_t g = 0; g < o.bic_rows.size(); ++g) {
+        regA2[k].push_back(static_cast<int64_t>(off2));
+        eA2[k].push_back(expo);
+        int32_t const rows = static_cast<int32_t>(o.bic_rows[g].size()) * eds;
+        for (size_t mi = 0; mi < o.bic_rows[g].size(); ++mi) {
+          auto const &q = s.q2m[o.bic_rows[g][mi]];
+          int32_t const p = o.pairs.at({q.b1, q.r1}), ci = o.codes.at(q.vdv);
+          for (int32_t a = 0; a < eds; ++a) {
+            int32_t const r = a / dilE;
+            dev::GVec v{};
+            v.dst = static_cast<int64_t>(off2);
+            v.stride = ld;
+            v.row = static_cast<int32_t>(mi) * eds + a;
+            v.expo = expo++;
+            v.n_seg = 4;
+            v.seg_len = nev;
+            for (int32_t bd = 0; bd < 4; ++bd) {
+              bool const flip = (bd + r == 3) || (bd - r > 1) || (r - bd > 1);
+              v.seg[bd].src = o.q2m + ((p * eds + a) * 4 + bd) + ld * (static_cast<int64_t>(ci) * nev);
+              v.seg[bd].factor = flip ? 2 : 0;
+            }
+            vec.push_back(v);
+          }
+        }
+        off2 += dev::tc_a_bytes(rows, kt2);
+      }
+    }
+    end(b.a_q2);
+    begin(b.b_q2);
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      int const t = batch_ts[k];
+      TOut &o = tos[k];
+      for (size_t g = 0; g < o.bic_cols.size(); ++g) {
+        regB2[k].push_back(static_cast<int64_t>(off2));
+        eB2[k].push_back(expo);
+        int32_t const cols = static_cast<int32_t>(o.bic_cols[g].size()) * eds;
+        for (size_t ci = 0; ci < o.bic_cols[g].size(); ++ci) {
+          auto const &cg = o.bic_cols[g][ci];  // (gamma, r2, b2)
+          for (int32_t c = 0; c < eds; ++c) {
+            dev::GVec v{};
+            v.dst = static_cast<int64_t>(off2);
+            v.stride = 1;
+            v.row = static_cast<int32_t>(ci) * eds + c;
+            v.expo = expo++;
+            v.n_seg = 4;
+            v.seg_len = nev;
+            for (int32_t bd = 0; bd < 4; ++bd) {
+              v.seg[bd].src = cg[1] * prs + (4LL * t + dev::gamma_row_host(cg[0], bd)) * nev +
+                              prow * (static_cast<int64_t>(cg[2]) * eds + c);
+              v.seg[bd].factor = dev::gamma_phase_host(cg[0], bd);
+            }
+            vec.push_back(v);
+          }
+        }
+        off2 += dev::tc_b_bytes(cols, kt2);
+      }
+    }
+    end(b.b_q2);
+    b.t2[0] = static_cast<int64_t>(tiles.size());
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      TOut &o = tos[k];
+      for (size_t g = 0; g < o.bic_rows.size(); ++g) {
+        int32_t const rows = static_cast<int32_t>(o.bic_rows[g].size()) * eds;
+        int32_t const cols = static_cast<int32_t>(o.bic_cols[g].size()) * eds;
+        out2[k].push_back(out);
+        add_tiles(regA2[k][g], regB2[k][g], a_tile2, b_tile2, rows, cols, out, eA2[k][g],
+                  eB2[k][g]);
+        out += static_cast<int64_t>(rows) * cols;
+      }
+    }
+    b.t2[1] = static_cast<int64_t>(tiles.size()) - b.t2[0];
+    need = std::max(need, off2);
+    // -- gathers
+    b.g1[0] = static_cast<int64_t>(g1.size());
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      TOut &o = tos[k];
+      for (int32_t qi : q1_t[batch_ts[k]]) {
+        auto const &q = s.q1[qi];
+        dev::Q1Gather g{};
+        g.x_off = o.x1;
+        g.ld = o.x1_rows;
+        g.row0 = o.rloc.at(q.r) * eds;
+        g.col0 = (q.r2 * nb + q.b) * 4 * eds;
+        g.gamma = q.gamma;
+        g.slot = q.slot;
+        g1.push_back(g);
+      }
+    }
+    b.g1[1] = static_cast<int64_t>(g1.size()) - b.g1[0];
+    b.g2[0] = static_cast<int64_t>(g2.size());
+    for (size_t k = 0; k < batch_ts.size(); ++k) {
+      TOut &o = tos[k];
+      std::map<int32_t, std::pair<size_t, size_t>> where;  // Q2M m -> (biclique, row)
+      for (size_t g = 0; g < o.bic_rows.size(); ++g)
+        for (size_t mi = 0; mi < o.bic_rows[g].size(); ++mi) where[o.bic_rows[g][mi]] = {g, mi};
+      for (int32_t qi : q2_t[batch_ts[k]]) {
+        auto const &q = s.q2[qi];
+        auto const w = where.at(q.m);
+        auto const &cols = o.bic_cols[w.first];
+        std::array<int32_t, 3> const key{q.gamma, q.r2, q.b2};
+        size_t const ci = std::lower_bound(cols.begin(), cols.end(), key) - cols.begin();
+        int32_t const rows = static_cast<int32_t>(o.bic_rows[w.first].size()) * eds;
+        dev::Q2Gather g{};
+        g.off = out2[k][w.first] + static_cast<int64_t>(w.second) * eds +
+                static_cast<int64_t>(rows) * (static_cast<int64_t>(ci) * eds);
+        g.ld = rows;
+        g.slot = q.slot;
+        g2.push_back(g);
+      }
+    }
+    b.g2[1] = static_cast<int64_t>(g2.size()) - b.g2[0];
+    need_out = std::max(need_out, out);
+    need_expo = std::max<int64_t>(need_expo, expo);
+    ds.f_batches.push_back(b);
+    batch_ts.clear();
+    used1 = used2 = 0;
+    used_out = 0;
+  };
+  std::vector<std::vector<int32_t>> br;
+  std::vector<std::vector<std::array<int32_t, 3>>> bc;
+  for (int t = 0; t < Lt; ++t) {
+    if (q1r_t[t].empty() && q2m_t[t].empty() && q2_t[t].empty()) continue;
+    TPlan const p = t_sizes(t, br, bc);
+    if (!batch_ts.empty() &&
+        (used1 + p.s1 > cap || used2 + p.s2 > cap || used_out + p.out > out_cap))
+      flush();
+    batch_ts.push_back(t);
+    used1 += p.s1;
+    used2 += p.s2;
+    used_out += p.out;
+  }
+  flush();
+  upload(ds.fvec, vec, stream_);
+  upload(ds.ftiles, tiles, stream_);
+  upload(ds.fg1, g1, stream_);
+  upload(ds.fg2, g2, stream_);
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  ds.f_scratch = need;
+  ds.f_out = need_out;
+  ds.f_expo = need_expo;
+  ds.f_ready = true;
+}
+
 void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
                       int single_block_pair, double *corr_out) {
   if (!plan || !corr_out) throw ArgError("null plan or output");
@@ -481,26 +878,71 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     df_slots_t_.reserve(df_bytes);
     int64_t const n_vdv = 2LL * static_cast<int64_t>(ops_.size()) * dims_.Lt * nev * nev;
     int64_t const n_noise = 4LL * nev * dims_.Lt * dims_.n_rnd;
-    int64_t const n_peram = peram_elems() * dims_.n_rnd;
-    DevBuf vdv_df, noise_df, peram_df, q0m, q1r, q2m;
+    DevBuf vdv_df, noise_df, q0m, q1r;
     vdv_df.reserve(sizeof(float4) * std::max<int64_t>(1, n_vdv));
     noise_df.reserve(sizeof(float4) * n_noise);
-    peram_df.reserve(sizeof(float4) * n_peram);
     launch(dev::to_df(vdv_df.as<float4>(), vdv_.as<double2>(), n_vdv, stream_), "to_df");
     launch(dev::to_df(noise_df.as<float4>(), noise_.as<double2>(), n_noise, stream_), "to_df");
-    launch(dev::to_df(peram_df.as<float4>(), peram_.as<double2>(), n_peram, stream_), "to_df");
     q0m.reserve(sizeof(float4) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
     q1r.reserve(sizeof(float4) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
-    q2m.reserve(sizeof(float4) * std::max<int64_t>(1, s.q2m.size()) * eds * 4 * nev);
+    // Q0 and the Q1R intermediates in double-float; Q2M, Q1 and Q2 on the
+    // tensor cores below.
     launch(dev::factors_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), q0m.as<float4>(),
-                           q1r.as<float4>(), q2m.as<float4>(), ds.q0m.as<dev::Q0MInst>(),
-                           s.q0m.size(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(),
-                           ds.q2m.as<dev::Q2MInst>(), s.q2m.size(), ds.q0.as<dev::Q0Inst>(),
-                           s.q0.size(), ds.q1.as<dev::Q1Inst>(), s.q1.size(),
-                           ds.q2.as<dev::Q2Inst>(), s.q2.size(), vdv_df.as<float4>(),
-                           noise_df.as<float4>(), peram_df.as<float4>(), geo_, stream_),
+                           q1r.as<float4>(), nullptr, ds.q0m.as<dev::Q0MInst>(),
+                           s.q0m.size(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(), nullptr, 0,
+                           ds.q0.as<dev::Q0Inst>(), s.q0.size(), nullptr, 0, nullptr, 0,
+                           vdv_df.as<float4>(), noise_df.as<float4>(), nullptr, geo_, stream_),
            "factors_df");
-    launches_ += 5;
+    launches_ += 2;
+    prepare_factor_tc(ds);
+    tc_scratch_.reserve(std::max<size_t>(1, ds.f_scratch));
+    f_out_.reserve(sizeof(double2) * std::max<int64_t>(1, ds.f_out));
+    tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, ds.f_expo));
+    err_.reserve(sizeof(int));
+    SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
+    int32_t const kt1 = dev::gemm_k_tiles(nev), kt2 = dev::gemm_k_tiles(4 * nev);
+    uint8_t *scr = tc_scratch_.as<uint8_t>();
+    int32_t *ex = tr_expo_.as<int32_t>();
+    double2 *fo = f_out_.as<double2>();
+    auto const *fv = ds.fvec.as<dev::GVec>();
+    auto const *ft = ds.ftiles.as<dev::TrTile>();
+    auto count = [&](int64_t n) { launches_ += n > 0 ? 1 : 0; };
+    for (auto const &b : ds.f_batches) {
+      cuda_check(dev::gvec_slice_df(scr, ex, fv + b.a_x1[0], b.a_x1[1], true, true,
+                                    q1r.as<float4>(), kt1, stream_),
+                 "slice X1 A");
+      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.a_q2m[0], b.a_q2m[1], true, false,
+                                     peram_.as<double2>(), kt1, stream_),
+                 "slice Q2M A");
+      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_x1[0], b.b_x1[1], false, false,
+                                     peram_.as<double2>(), kt1, stream_),
+                 "slice X1 B");
+      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_q2m[0], b.b_q2m[1], false, false,
+                                     vdv_.as<double2>(), kt1, stream_),
+                 "slice Q2M B");
+      count(b.a_x1[1]); count(b.a_q2m[1]); count(b.b_x1[1]); count(b.b_q2m[1]);
+      cuda_check(dev::tc_gemm(fo, scr, ex, ft + b.t1[0], b.t1[1], kt1, err_.as<int>(), stream_),
+                 "factor GEMM (X1, Q2M)");
+      count(b.t1[1]);
+      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.a_q2[0], b.a_q2[1], true, true, fo, kt2,
+                                     stream_),
+                 "slice Q2 A");
+      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_q2[0], b.b_q2[1], false, false,
+                                     peram_.as<double2>(), kt2, stream_),
+                 "slice Q2 B");
+      count(b.a_q2[1]); count(b.b_q2[1]);
+      cuda_check(dev::tc_gemm(fo, scr, ex, ft + b.t2[0], b.t2[1], kt2, err_.as<int>(), stream_),
+                 "factor GEMM (Q2)");
+      count(b.t2[1]);
+      cuda_check(dev::q1_gather(df_slots_.as<float4>(), df_slots_t_.as<float4>(),
+                                ds.fg1.as<dev::Q1Gather>() + b.g1[0], b.g1[1], fo, dims_.dilE,
+                                stream_),
+                 "q1_gather");
+      cuda_check(dev::q2_gather(df_slots_.as<float4>(), df_slots_t_.as<float4>(),
+                                ds.fg2.as<dev::Q2Gather>() + b.g2[0], b.g2[1], fo, eds, stream_),
+                 "q2_gather");
+      count(b.g1[1]); count(b.g2[1]);
+    }
     SLAPH_CK(cudaEventRecord(ev_[1], stream_));
     SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
   }

@@ -57,6 +57,19 @@ struct DeviceSchedule {
   };
   std::vector<std::unique_ptr<WaveBufs>> waves;
   double plan_seconds = 0;
+  // Q1/Q2 factors on the tensor cores (mixed precision), in batches of
+  // timeslices.  Phase 1: X1 = Q1R x perambulator blocks and the Q2M
+  // intermediates (K = nev); phase 2: Q2 (K = 4 nev); then gathers into slots.
+  struct FBatch {
+    int64_t a_x1[2], a_q2m[2], b_x1[2], b_q2m[2], a_q2[2], b_q2[2];  // (offset, count) in fvec
+    int64_t t1[2], t2[2];  // in ftiles
+    int64_t g1[2], g2[2];  // in fg1 / fg2
+  };
+  bool f_ready = false;
+  std::vector<FBatch> f_batches;
+  DevBuf fvec, ftiles, fg1, fg2;
+  size_t f_scratch = 0;
+  int64_t f_out = 0, f_expo = 0;  // doubles2 of dense outputs, exponents per batch
   bool tc_ready = false;
   size_t tc_scratch = 0;   // bytes of scratch the batches need
   int64_t tc_expo = 0;     // exponents per batch (maximum)
@@ -94,7 +107,8 @@ class Engine {
   int64_t launches_ = 0;
 
   // Working buffers of the contraction.
-  DevBuf slots_, df_slots_, df_slots_t_, values_, values_df_, term_val_, running_, tr_expo_;
+  DevBuf slots_, df_slots_, df_slots_t_, values_, values_df_, term_val_, running_, tr_expo_,
+      f_out_;
 
   std::unique_ptr<DeviceSchedule> sched_;
   slaph_plan const *sched_plan_ = nullptr;
@@ -103,6 +117,7 @@ class Engine {
   int64_t peram_elems() const;
   void prepare_schedule(slaph_plan const *plan, int single_block_pair);
   void prepare_trace_tc(DeviceSchedule &ds);
+  void prepare_factor_tc(DeviceSchedule &ds);
   void launch(cudaError_t e, char const *what) {
     cuda_check(e, what);
     ++launches_;

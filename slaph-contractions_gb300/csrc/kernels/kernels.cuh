@@ -53,6 +53,10 @@ struct Geometry {
 };
 
 // Gamma table (src/Gamma.cpp:18-246) into constant memory.
+// Gamma_m column c: row of its nonzero, and its value as a phase code
+// (0: +1, 1: +i, 2: -1, 3: -i), for host-side planning.
+int32_t gamma_row_host(int32_t m, int32_t c);
+int32_t gamma_phase_host(int32_t m, int32_t c);
 cudaError_t upload_gamma(cudaStream_t stream);
 
 // exp(-i p.x) for every op: phase[op][x] (create_momenta,
@@ -168,6 +172,56 @@ cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSlice const *a_ite
 cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
                           TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,
                           cudaStream_t stream);
+
+// Generic form of the same GEMM (factor_tc.cu): k_tiles k-tiles of 16
+// complex entries; region sizes for `rows` A rows / `cols` B columns.
+size_t tc_a_bytes(int32_t rows, int32_t k_tiles);
+size_t tc_b_bytes(int32_t cols, int32_t k_tiles);
+int32_t gemm_k_tiles(int64_t K);
+cudaError_t tc_gemm(double2 *out, uint8_t const *scratch, int32_t const *expo,
+                    TrTile const *tiles, int64_t n_tiles, int32_t k_tiles, int *err,
+                    cudaStream_t stream);
+
+// One GEMM operand row (A) or column (B) gathered from up to four strided
+// segments of a source array, each with an exact factor (0: +1, 1: +i, 2: -1,
+// 3: -i).  K = n_seg * seg_len, zero-padded to the region's k-tiles.
+struct GSeg {
+  int64_t src;
+  int32_t factor;
+  int32_t pad;
+};
+constexpr int kGMaxSeg = 4;
+struct GVec {
+  int64_t dst;     // byte offset of the region in the scratch buffer
+  int64_t stride;  // element stride along K inside a segment
+  int32_t row;     // row (A) or column (B) within the region
+  int32_t expo;    // index of its exponent
+  int32_t n_seg, seg_len;
+  GSeg seg[kGMaxSeg];
+};
+// Slices operand vectors (A rows with put conj(v) when conj, or B columns)
+// from an FP64 or a double-float source.
+cudaError_t gvec_slice_f64(uint8_t *scratch, int32_t *expo, GVec const *items, int64_t n,
+                           bool is_a, bool conj, double2 const *src, int32_t k_tiles,
+                           cudaStream_t stream);
+cudaError_t gvec_slice_df(uint8_t *scratch, int32_t *expo, GVec const *items, int64_t n,
+                          bool is_a, bool conj, float4 const *src, int32_t k_tiles,
+                          cudaStream_t stream);
+// Q1 factor slots from the dense product X1 (factor_tc.cu); Q2 slots from the
+// dense Q2 GEMM output.
+struct Q1Gather {
+  int64_t x_off;  // element offset of X1 of the factor's timeslice
+  int32_t ld, row0, col0, gamma, slot, pad;
+};
+struct Q2Gather {
+  int64_t off;  // element offset of the factor's (0, 0) entry
+  int32_t ld, slot;
+};
+cudaError_t upload_gamma_tc(cudaStream_t stream);
+cudaError_t q1_gather(float4 *sn, float4 *st, Q1Gather const *g, int64_t n, double2 const *x,
+                      int32_t dilE, cudaStream_t stream);
+cudaError_t q2_gather(float4 *sn, float4 *st, Q2Gather const *g, int64_t n, double2 const *y,
+                      int32_t eds, cudaStream_t stream);
 
 // values[i] = hi + lo of values_df[i] for i < n_values, the FP64 trace values
 // the terms read.

@@ -534,25 +534,35 @@ int blocks_for(int64_t n, int threads) {
 
 // The gamma table of src/Gamma.cpp:18-246 (tmLQCD basis): for matrix m and
 // column c the non-zero row and its value (+-1, +-i).
+namespace {
+// Gamma table (the data of src/Gamma.cpp:18-246): Gamma_m has, in column c, its
+// single nonzero at row kGammaRow[m][c] with value kGammaVal[m][c] (re, im).
+int32_t const kGammaRow[16][4] = {{2, 3, 0, 1}, {3, 2, 1, 0}, {3, 2, 1, 0}, {2, 3, 0, 1},
+                                  {0, 1, 2, 3}, {0, 1, 2, 3}, {2, 3, 0, 1}, {3, 2, 1, 0},
+                                  {3, 2, 1, 0}, {2, 3, 0, 1}, {1, 0, 3, 2}, {1, 0, 3, 2},
+                                  {0, 1, 2, 3}, {1, 0, 3, 2}, {1, 0, 3, 2}, {0, 1, 2, 3}};
+double const kGammaVal[16][4][2] = {
+    {{1, 0}, {1, 0}, {1, 0}, {1, 0}},      {{0, -1}, {0, -1}, {0, 1}, {0, 1}},
+    {{1, 0}, {-1, 0}, {-1, 0}, {1, 0}},    {{0, -1}, {0, 1}, {0, 1}, {0, -1}},
+    {{1, 0}, {1, 0}, {1, 0}, {1, 0}},      {{1, 0}, {1, 0}, {-1, 0}, {-1, 0}},
+    {{1, 0}, {1, 0}, {-1, 0}, {-1, 0}},    {{0, -1}, {0, -1}, {0, -1}, {0, -1}},
+    {{1, 0}, {-1, 0}, {1, 0}, {-1, 0}},    {{0, -1}, {0, 1}, {0, -1}, {0, 1}},
+    {{0, -1}, {0, -1}, {0, 1}, {0, 1}},    {{1, 0}, {-1, 0}, {-1, 0}, {1, 0}},
+    {{0, -1}, {0, 1}, {0, 1}, {0, -1}},    {{0, -1}, {0, -1}, {0, -1}, {0, -1}},
+    {{1, 0}, {-1, 0}, {1, 0}, {-1, 0}},    {{0, -1}, {0, 1}, {0, -1}, {0, 1}}};
+}  // namespace
+
+int32_t gamma_row_host(int32_t m, int32_t c) { return kGammaRow[m][c]; }
+int32_t gamma_phase_host(int32_t m, int32_t c) {
+  double const re = kGammaVal[m][c][0], im = kGammaVal[m][c][1];
+  return re > 0 ? 0 : im > 0 ? 1 : re < 0 ? 2 : 3;
+}
+
 cudaError_t upload_gamma(cudaStream_t stream) {
-  static int32_t const row[16][4] = {{2, 3, 0, 1}, {3, 2, 1, 0}, {3, 2, 1, 0}, {2, 3, 0, 1},
-                                     {0, 1, 2, 3}, {0, 1, 2, 3}, {2, 3, 0, 1}, {3, 2, 1, 0},
-                                     {3, 2, 1, 0}, {2, 3, 0, 1}, {1, 0, 3, 2}, {1, 0, 3, 2},
-                                     {0, 1, 2, 3}, {1, 0, 3, 2}, {1, 0, 3, 2}, {0, 1, 2, 3}};
-  // value as (re, im)
-  static double const val[16][4][2] = {
-      {{1, 0}, {1, 0}, {1, 0}, {1, 0}},      {{0, -1}, {0, -1}, {0, 1}, {0, 1}},
-      {{1, 0}, {-1, 0}, {-1, 0}, {1, 0}},    {{0, -1}, {0, 1}, {0, 1}, {0, -1}},
-      {{1, 0}, {1, 0}, {1, 0}, {1, 0}},      {{1, 0}, {1, 0}, {-1, 0}, {-1, 0}},
-      {{1, 0}, {1, 0}, {-1, 0}, {-1, 0}},    {{0, -1}, {0, -1}, {0, -1}, {0, -1}},
-      {{1, 0}, {-1, 0}, {1, 0}, {-1, 0}},    {{0, -1}, {0, 1}, {0, -1}, {0, 1}},
-      {{0, -1}, {0, -1}, {0, 1}, {0, 1}},    {{1, 0}, {-1, 0}, {-1, 0}, {1, 0}},
-      {{0, -1}, {0, 1}, {0, 1}, {0, -1}},    {{0, -1}, {0, -1}, {0, -1}, {0, -1}},
-      {{1, 0}, {-1, 0}, {1, 0}, {-1, 0}},    {{0, -1}, {0, 1}, {0, -1}, {0, 1}}};
   double2 v[16][4];
   for (int m = 0; m < 16; ++m)
-    for (int c = 0; c < 4; ++c) v[m][c] = make_double2(val[m][c][0], val[m][c][1]);
-  cudaError_t e = cudaMemcpyToSymbolAsync(c_gamma_row, row, sizeof row, 0,
+    for (int c = 0; c < 4; ++c) v[m][c] = make_double2(kGammaVal[m][c][0], kGammaVal[m][c][1]);
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_gamma_row, kGammaRow, sizeof kGammaRow, 0,
                                           cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbolAsync(c_gamma_val, v, sizeof v, 0, cudaMemcpyHostToDevice, stream);

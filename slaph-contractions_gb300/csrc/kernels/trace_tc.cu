@@ -126,17 +126,32 @@ cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSlice const *a_ite
   return cudaGetLastError();
 }
 
-cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
-                          TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,
-                          cudaStream_t stream) {
+size_t tc_a_bytes(int32_t rows, int32_t k_tiles) {
+  return static_cast<size_t>((rows + kTM / 2 - 1) / (kTM / 2)) * k_tiles * kStageA;
+}
+size_t tc_b_bytes(int32_t cols, int32_t k_tiles) {
+  return static_cast<size_t>((cols + kTN - 1) / kTN) * k_tiles * kStageB;
+}
+
+cudaError_t tc_gemm(double2 *out, uint8_t const *scratch, int32_t const *expo,
+                    TrTile const *tiles, int64_t n_tiles, int32_t k_tiles, int *err,
+                    cudaStream_t stream) {
   if (n_tiles == 0) return cudaSuccess;
+  if (k_tiles < 1) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(trace_gemm_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(kSmemBytes));
   if (e != cudaSuccess) return e;
   trace_gemm_kernel<<<static_cast<unsigned>(n_tiles), kThreads, kSmemBytes, stream>>>(
-      values, scratch, expo, tiles, static_cast<int32_t>(trace_tc_k_tiles(eds)), err);
+      out, scratch, expo, tiles, k_tiles, err);
   return cudaGetLastError();
+}
+
+cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
+                          TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,
+                          cudaStream_t stream) {
+  return tc_gemm(values, scratch, expo, tiles, n_tiles,
+                 static_cast<int32_t>(trace_tc_k_tiles(eds)), err, stream);
 }
 
 }  // namespace dev

@@ -27,6 +27,32 @@ def _c128(a):
     return a
 
 
+class _PinnedBlock:
+    """Owner of one slaph_host_alloc block; freed when the last view goes."""
+
+    def __init__(self, nbytes):
+        p = C.c_void_p()
+        L.check(L.lib().slaph_host_alloc(nbytes, C.byref(p)))
+        self.ptr = p.value
+        self.nbytes = nbytes
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            L.lib().slaph_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.complex128):
+    """A numpy array in driver-pinned host memory (slaph_host_alloc), for
+    inputs that are uploaded every configuration."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    blk = _PinnedBlock(max(n, 1))
+    buf = (C.c_char * max(n, 1)).from_address(blk.ptr)
+    buf._owner = blk  # keeps the block alive as long as any view of buf
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+
 class Engine:
     """One engine per lattice geometry (slaph_engine_*)."""
 
