@@ -219,10 +219,24 @@ int slaph_engine_destroy(slaph_engine *eng);
  * (create_momenta, src/OperatorFactory.cpp:64-95). */
 int slaph_engine_set_operators(slaph_engine *eng, const slaph_vdv_op *ops, int32_t n_ops,
                                int32_t index_of_unity);
-/* Host -> device copies of the inputs (layouts as the readers above). */
+/* Host -> device copies of the inputs (layouts as the readers above).  The
+ * plain forms return when the copy is done.  The _async forms only enqueue it
+ * on the engine's upload stream and return at once: slaph_vdaggerv_build then
+ * waits for each eigenvector timeslice just before it needs it (overlapping
+ * the remaining copies with VdaggerV work) and slaph_contract for the
+ * perambulators and noise.  The host buffer of an _async call must stay valid
+ * and unchanged until the build (eigenvectors) or contract (perambulators,
+ * noise) that consumes it returns; page-locked buffers (slaph_host_alloc) make
+ * the copy asynchronous, pageable ones are copied before the call returns.
+ * The reference reads each eigenvector timeslice inside the VdaggerV loop
+ * (src/OperatorFactory.cpp:274-278); these calls are the device-side
+ * counterpart of that overlap. */
 int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V);
 int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram);
 int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise);
+int slaph_engine_set_eigenvectors_async(slaph_engine *eng, int32_t t, const double *V);
+int slaph_engine_set_perambulator_async(slaph_engine *eng, int32_t rnd_id, const double *peram);
+int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id, const double *noise);
 
 /* Page-locked host memory for the inputs, so that the set_* copies above run
  * at the full host-device link rate.  slaph_host_alloc returns driver-pinned

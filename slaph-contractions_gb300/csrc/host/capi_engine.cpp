@@ -50,6 +50,19 @@ int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const doub
   return slaph::guarded([&] { get(eng).set_random_vector(rnd_id, noise); });
 }
 
+int slaph_engine_set_eigenvectors_async(slaph_engine *eng, int32_t t, const double *V) {
+  return slaph::guarded([&] { get(eng).set_eigenvectors(t, V, true); });
+}
+
+int slaph_engine_set_perambulator_async(slaph_engine *eng, int32_t rnd_id, const double *peram) {
+  return slaph::guarded([&] { get(eng).set_perambulator(rnd_id, peram, true); });
+}
+
+int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id,
+                                         const double *noise) {
+  return slaph::guarded([&] { get(eng).set_random_vector(rnd_id, noise, true); });
+}
+
 int slaph_host_alloc(size_t bytes, void **out) {
   return slaph::guarded([&] {
     if (!out || bytes == 0) throw slaph::ArgError("null output or empty size");

@@ -88,7 +88,22 @@ Engine::Engine(slaph_dims const &d) : dims_(d) {
   geo_.dim_row = 3LL * d.Lx * d.Ly * d.Lz;
   SLAPH_CK(cudaGetDevice(&device_));
   SLAPH_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  SLAPH_CK(cudaStreamCreateWithFlags(&up_stream_, cudaStreamNonBlocking));
   for (auto &e : ev_) SLAPH_CK(cudaEventCreate(&e));
+  auto make_events = [](std::vector<cudaEvent_t> &v, int n) {
+    v.assign(n, nullptr);
+    for (auto &e : v) SLAPH_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  };
+  make_events(ev_v_, d.Lt);
+  make_events(ev_p_, d.n_rnd);
+  make_events(ev_n_, d.n_rnd);
+  pend_v_.assign(d.Lt, 0);
+  pend_p_.assign(d.n_rnd, 0);
+  pend_n_.assign(d.n_rnd, 0);
+  SLAPH_CK(cudaEventCreateWithFlags(&ev_v_used_, cudaEventDisableTiming));
+  SLAPH_CK(cudaEventCreateWithFlags(&ev_pn_used_, cudaEventDisableTiming));
+  SLAPH_CK(cudaEventRecord(ev_v_used_, stream_));
+  SLAPH_CK(cudaEventRecord(ev_pn_used_, stream_));
   V_.reserve(sizeof(double2) * geo_.dim_row * d.nev * d.Lt);
   peram_.reserve(sizeof(double2) * peram_elems() * d.n_rnd);
   noise_.reserve(sizeof(double2) * 4LL * d.nev * d.Lt * d.n_rnd);
@@ -100,9 +115,16 @@ Engine::Engine(slaph_dims const &d) : dims_(d) {
 }
 
 Engine::~Engine() {
+  if (up_stream_) cudaStreamSynchronize(up_stream_);
   if (stream_) cudaStreamSynchronize(stream_);
   for (auto &e : ev_)
     if (e) cudaEventDestroy(e);
+  for (auto *v : {&ev_v_, &ev_p_, &ev_n_})
+    for (auto &e : *v)
+      if (e) cudaEventDestroy(e);
+  if (ev_v_used_) cudaEventDestroy(ev_v_used_);
+  if (ev_pn_used_) cudaEventDestroy(ev_pn_used_);
+  if (up_stream_) cudaStreamDestroy(up_stream_);
   for (auto &e : tc_ev_)
     if (e) cudaEventDestroy(e);
   if (stream_) cudaStreamDestroy(stream_);
@@ -141,29 +163,39 @@ void Engine::set_operators(slaph_vdv_op const *ops, int32_t n, int32_t index_of_
   vdv_built_ = false;
 }
 
-void Engine::set_eigenvectors(int32_t t, double const *V) {
+void Engine::set_eigenvectors(int32_t t, double const *V, bool async) {
   if (t < 0 || t >= dims_.Lt || !V) throw ArgError("invalid timeslice or null pointer");
   size_t const n = static_cast<size_t>(geo_.dim_row) * dims_.nev;
+  // The previous VdaggerV build must be done with V before it is overwritten.
+  SLAPH_CK(cudaStreamWaitEvent(up_stream_, ev_v_used_, 0));
   SLAPH_CK(cudaMemcpyAsync(V_.as<double2>() + n * t, V, n * sizeof(double2),
-                           cudaMemcpyHostToDevice, stream_));
-  SLAPH_CK(cudaStreamSynchronize(stream_));
+                           cudaMemcpyHostToDevice, up_stream_));
+  SLAPH_CK(cudaEventRecord(ev_v_[t], up_stream_));
+  pend_v_[t] = 1;
+  if (!async) SLAPH_CK(cudaEventSynchronize(ev_v_[t]));
   vdv_built_ = false;
 }
 
-void Engine::set_perambulator(int32_t r, double const *P) {
+void Engine::set_perambulator(int32_t r, double const *P, bool async) {
   if (r < 0 || r >= dims_.n_rnd || !P) throw ArgError("invalid random vector index");
   size_t const n = static_cast<size_t>(peram_elems());
+  SLAPH_CK(cudaStreamWaitEvent(up_stream_, ev_pn_used_, 0));
   SLAPH_CK(cudaMemcpyAsync(peram_.as<double2>() + n * r, P, n * sizeof(double2),
-                           cudaMemcpyHostToDevice, stream_));
-  SLAPH_CK(cudaStreamSynchronize(stream_));
+                           cudaMemcpyHostToDevice, up_stream_));
+  SLAPH_CK(cudaEventRecord(ev_p_[r], up_stream_));
+  pend_p_[r] = 1;
+  if (!async) SLAPH_CK(cudaEventSynchronize(ev_p_[r]));
 }
 
-void Engine::set_random_vector(int32_t r, double const *noise) {
+void Engine::set_random_vector(int32_t r, double const *noise, bool async) {
   if (r < 0 || r >= dims_.n_rnd || !noise) throw ArgError("invalid random vector index");
   size_t const n = 4ULL * dims_.nev * dims_.Lt;
+  SLAPH_CK(cudaStreamWaitEvent(up_stream_, ev_pn_used_, 0));
   SLAPH_CK(cudaMemcpyAsync(noise_.as<double2>() + n * r, noise, n * sizeof(double2),
-                           cudaMemcpyHostToDevice, stream_));
-  SLAPH_CK(cudaStreamSynchronize(stream_));
+                           cudaMemcpyHostToDevice, up_stream_));
+  SLAPH_CK(cudaEventRecord(ev_n_[r], up_stream_));
+  pend_n_[r] = 1;
+  if (!async) SLAPH_CK(cudaEventSynchronize(ev_n_[r]));
 }
 
 void Engine::vdaggerv_build(int precision) {
@@ -186,20 +218,32 @@ void Engine::vdaggerv_build(int precision) {
     SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
   }
   SLAPH_CK(cudaEventRecord(ev_[0], stream_));
+  // Eigenvectors uploaded asynchronously: the split-precision build waits for
+  // each timeslice just before slicing it (overlapping the remaining copies),
+  // the FP64 build for all of them.
+  std::vector<cudaEvent_t> ready(dims_.Lt, nullptr);
+  for (int32_t t = 0; t < dims_.Lt; ++t)
+    if (pend_v_[t]) ready[t] = ev_v_[t];
   if (precision == SLAPH_MIXED) {
     launch(dev::vdaggerv_tc(vdv_.as<double2>(), V_.as<double2>(), phase_fx_.as<longlong2>(),
                             list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_,
-                            tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_),
+                            tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_,
+                            ready.data()),
            "vdaggerv_tc");
     // three slicing kernels per timeslice, one GEMM per timeslice batch
     int64_t const per = static_cast<int64_t>(
         tc_scratch_.size() / dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_comp, 1), 1));
     launches_ += 3LL * dims_.Lt + (dims_.Lt + per - 1) / std::max<int64_t>(per, 1) - 1;
   } else {
+    for (auto e : ready)
+      if (e) SLAPH_CK(cudaStreamWaitEvent(stream_, e, 0));
     launch(dev::vdaggerv_fp64(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
                               list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_, stream_),
            "vdaggerv_fp64");
   }
+  // V is not read after this point: later uploads may overwrite it.
+  SLAPH_CK(cudaEventRecord(ev_v_used_, stream_));
+  std::fill(pend_v_.begin(), pend_v_.end(), 0);
   if (index_of_unity_ >= 0)
     launch(dev::vdaggerv_identity(vdv_.as<double2>(), index_of_unity_, geo_, stream_),
            "vdaggerv_identity");
@@ -841,6 +885,13 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
 
   // ---- factors
   bool const mixed = precision == SLAPH_MIXED;
+  // Perambulators and noise uploaded asynchronously are waited for here.
+  for (int32_t r = 0; r < dims_.n_rnd; ++r) {
+    if (pend_p_[r]) SLAPH_CK(cudaStreamWaitEvent(stream_, ev_p_[r], 0));
+    if (pend_n_[r]) SLAPH_CK(cudaStreamWaitEvent(stream_, ev_n_[r], 0));
+  }
+  std::fill(pend_p_.begin(), pend_p_.end(), 0);
+  std::fill(pend_n_.begin(), pend_n_.end(), 0);
   SLAPH_CK(cudaEventRecord(ev_[0], stream_));
   if (!mixed) {
     slots_.reserve(sizeof(double2) * ms *
@@ -947,6 +998,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
   }
   timings[1] = elapsed_ms(ev_[0], ev_[1]);
+  // Perambulators and noise are not read after the factor stage.
+  SLAPH_CK(cudaEventRecord(ev_pn_used_, stream_));
 
   // ---- waves: products, traces, terms, accumulation
   values_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_values));

@@ -81,9 +81,12 @@ class Engine {
   ~Engine();
 
   void set_operators(slaph_vdv_op const *ops, int32_t n, int32_t index_of_unity);
-  void set_eigenvectors(int32_t t, double const *V);
-  void set_perambulator(int32_t r, double const *peram);
-  void set_random_vector(int32_t r, double const *noise);
+  // Host -> device copies on the upload stream; the blocking forms wait for
+  // their copy, the asynchronous ones return at once (the host buffer must stay
+  // valid until the next vdaggerv_build / contract that consumes it returns).
+  void set_eigenvectors(int32_t t, double const *V, bool async = false);
+  void set_perambulator(int32_t r, double const *peram, bool async = false);
+  void set_random_vector(int32_t r, double const *noise, bool async = false);
   void vdaggerv_build(int precision);
   void vdaggerv_fetch(int32_t op, int32_t t, double *out);
   void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
@@ -98,6 +101,12 @@ class Engine {
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev_[8] = {};
+  // Input uploads: their own stream, one completion event per timeslice /
+  // random vector, and the compute stream's last use of each input buffer.
+  cudaStream_t up_stream_ = nullptr;
+  std::vector<cudaEvent_t> ev_v_, ev_p_, ev_n_;
+  std::vector<char> pend_v_, pend_p_, pend_n_;
+  cudaEvent_t ev_v_used_ = nullptr, ev_pn_used_ = nullptr;
   std::vector<cudaEvent_t> tc_ev_;  // three per tensor-core trace batch
 
   DevBuf V_, peram_, noise_, phase_, phase_fx_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;

@@ -83,7 +83,10 @@ cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
 int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes);
 cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_fx,
                         int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
-                        void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream);
+                        void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
+                        cudaEvent_t const *t_ready = nullptr);
+// (t_ready[t], when given and non-null: event after which timeslice t of V is
+// valid; the slicing of t waits for it on `stream`.)
 // Identity blocks for code 2*op (and 2*op+1).
 cudaError_t vdaggerv_identity(double2 *vdv, int32_t op, Geometry g, cudaStream_t stream);
 // vdv[2*op+1][t] = vdv[2*op][t]^H for all ops, t.

@@ -182,7 +182,8 @@ cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
 
 cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_fx,
                         int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
-                        void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream) {
+                        void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
+                        cudaEvent_t const *t_ready) {
   if (n == 0 || nt == 0) return cudaSuccess;
   TcLayout const L = tc_layout(g, n);
   if (L.k_tiles > 0x7fffffffLL / kTK) return cudaErrorInvalidValue;
@@ -202,6 +203,10 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
   for (int32_t tb = t0; tb < t0 + nt; tb += static_cast<int32_t>(batch)) {
     int32_t const nb = static_cast<int32_t>(std::min<int64_t>(batch, t0 + nt - tb));
     for (int32_t b = 0; b < nb; ++b) {
+      if (t_ready && t_ready[tb + b]) {
+        e = cudaStreamWaitEvent(stream, t_ready[tb + b], 0);
+        if (e != cudaSuccess) return e;
+      }
       double2 const *Vt = V + static_cast<int64_t>(tb + b) * g.nev * g.dim_row;
       uint8_t *slot = base + b * L.slot_bytes;
       int32_t *expo = reinterpret_cast<int32_t *>(slot + L.e_off);

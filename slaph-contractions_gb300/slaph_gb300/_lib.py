@@ -109,6 +109,9 @@ PROTOTYPES = {
     "slaph_engine_set_eigenvectors": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_engine_set_perambulator": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_engine_set_random_vector": (C.c_int, [C.c_void_p, _i32, _dp]),
+    "slaph_engine_set_eigenvectors_async": (C.c_int, [C.c_void_p, _i32, _dp]),
+    "slaph_engine_set_perambulator_async": (C.c_int, [C.c_void_p, _i32, _dp]),
+    "slaph_engine_set_random_vector_async": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_vdaggerv_build": (C.c_int, [C.c_void_p, C.c_int]),
     "slaph_vdaggerv_fetch": (C.c_int, [C.c_void_p, _i32, _i32, _dp]),
     "slaph_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),

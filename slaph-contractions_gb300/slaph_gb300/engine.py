@@ -77,18 +77,26 @@ class Engine:
         L.check(L.lib().slaph_engine_set_operators(self._h, plan.vdv_ops, plan.n_vdv_ops,
                                                    plan.index_of_unity))
 
-    def set_eigenvectors(self, t, V):
-        """V: timeslice t, complex (nev, 3L^3) C-order == (3L^3 x nev) column-major."""
+    def set_eigenvectors(self, t, V, asynchronous=False):
+        """V: timeslice t, complex (nev, 3L^3) C-order == (3L^3 x nev) column-major.
+        asynchronous: enqueue the copy only; V must stay alive and unchanged until
+        the next vdaggerv_build returns (see slaph_engine_set_eigenvectors_async)."""
         V = _c128(V)
-        L.check(L.lib().slaph_engine_set_eigenvectors(self._h, t, L.dptr(V)))
+        fn = (L.lib().slaph_engine_set_eigenvectors_async if asynchronous
+              else L.lib().slaph_engine_set_eigenvectors)
+        L.check(fn(self._h, t, L.dptr(V)))
 
-    def set_perambulator(self, r, P):
+    def set_perambulator(self, r, P, asynchronous=False):
         P = _c128(P)
-        L.check(L.lib().slaph_engine_set_perambulator(self._h, r, L.dptr(P)))
+        fn = (L.lib().slaph_engine_set_perambulator_async if asynchronous
+              else L.lib().slaph_engine_set_perambulator)
+        L.check(fn(self._h, r, L.dptr(P)))
 
-    def set_random_vector(self, r, noise):
+    def set_random_vector(self, r, noise, asynchronous=False):
         noise = _c128(noise)
-        L.check(L.lib().slaph_engine_set_random_vector(self._h, r, L.dptr(noise)))
+        fn = (L.lib().slaph_engine_set_random_vector_async if asynchronous
+              else L.lib().slaph_engine_set_random_vector)
+        L.check(fn(self._h, r, L.dptr(noise)))
 
     @staticmethod
     def pin(arr):
