@@ -13,10 +13,11 @@
 //   largest |entry|) and cut into 6 signed slices of at most 8 bits:
 //   x = sum_p a_p 2^(-7-8(p-1)), a_p integer in [-128, 128], exact in BF16.
 //   47 bits are kept.
-// * Exact FP32 accumulation.  Slice products a_p b_q (|.| <= 2^14) of the same
+// * FP32 accumulation.  Slice products a_p b_q (|.| <= 2^14) of the same
 //   scale level l = p + q are accumulated in one TMEM accumulator.  Over a chunk
-//   of 256 K' values the levels 2..5 stay below 2^24 and are exact; levels 6, 7
-//   (scale <= 2^-32) carry FP32 rounding far below the target.  21 pairs
+//   of 512 K' values the levels 2 and 3 (one and two slice pairs) stay within
+//   2^24 and are exact; the lower levels (scale <= 2^-16) can round only by
+//   2^-24 of their own magnitude, at most 2^-40 of the row scale.  21 pairs
 //   (p + q <= 7), 6 accumulators.
 // * Promotion.  After every chunk the 6 accumulators are read from TMEM and
 //   added, scaled by 2^-8(l-2), into a double-float (two FP32) accumulator in
@@ -44,8 +45,8 @@ constexpr int kSlices = 6;
 constexpr int kTM = 128;       // rows of A' per tile (64 complex rows x re/im)
 constexpr int kTN = 80;        // columns of B per tile
 constexpr int kTK = 32;        // K' per k-tile (bf16 elements)
-constexpr int kChunkKT = 8;    // k-tiles per exact chunk (256 K')
-constexpr int kStages = 2;
+constexpr int kChunkKT = 16;   // k-tiles per chunk (512 K') between promotions
+constexpr int kStages = 2;     // (a 5-stage pipeline of 16-wide k-tiles measured slower)
 constexpr uint32_t kABlk = kTM * kTK * 2;            // 8192 B
 constexpr uint32_t kBBlk = kTN * kTK * 2;            // 5120 B
 constexpr uint32_t kStageA = kSlices * kABlk;        // 49152 B
