@@ -271,6 +271,18 @@ int slaph_contract(slaph_engine *eng, const slaph_plan *plan, int precision, int
 /* Number of doubles slaph_contract writes for this plan. */
 int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt);
 
+/* Host-only view of the schedule slaph_contract builds for a plan (no GPU
+ * needed): out[0] waves (block pairs), [1] trace lists, [2] lists with
+ * distinct operands, [3] of those outside dense groups, [4] dense groups,
+ * [5] trace entries, [6] entries after merging equal lists, [7] entries in
+ * dense groups, [8] correlator terms, [9] factor products, [10..12] Q0, Q1, Q2
+ * factors, [13] correlator requests, [14] (check_layout != 0) 1 if every
+ * trace-value index is written exactly once and every list reads the values
+ * of a list with its operands, else 0.  Writes min(n, 15) values. */
+int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
+                              int32_t single_block_pair, int32_t check_layout, double *out,
+                              int32_t n);
+
 /* Per-stage device times of the last build / contract, in milliseconds,
  * measured with CUDA events on the engine stream.  out[0] VdaggerV,
  * out[1] factors Q0/Q1/Q2, out[2] products + traces, out[3] assembly,

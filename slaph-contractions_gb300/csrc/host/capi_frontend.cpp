@@ -4,7 +4,10 @@
 #include <string>
 #include <vector>
 
+#include <map>
+#include <tuple>
 #include "capi_util.hpp"
+#include "schedule.hpp"
 #include "frontend.hpp"
 
 namespace slaph {
@@ -169,6 +172,70 @@ int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt) {
   int64_t n = 0;
   for (int32_t d = 0; d < plan->n_diagrams; ++d) n += plan->diagrams[d].n_requests;
   return n * Lt * 2;
+}
+
+int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
+                              int32_t single_block_pair, int32_t check_layout, double *out,
+                              int32_t n) {
+  return slaph::guarded([&] {
+    if (!dims || !plan || !out || n < 0) throw slaph::ArgError("null argument");
+    slaph::Schedule const s = slaph::build_schedule(*dims, *plan, single_block_pair);
+    double v[16] = {};
+    v[0] = static_cast<double>(s.waves.size());
+    int64_t lists = 0, uniq = 0, resid = 0, groups = 0;
+    for (auto const &w : s.waves) {
+      lists += static_cast<int64_t>(w.lists.size());
+      uniq += static_cast<int64_t>(w.unique_lists.size());
+      resid += static_cast<int64_t>(w.residual_lists.size());
+      groups += static_cast<int64_t>(w.groups.size());
+    }
+    v[1] = static_cast<double>(lists);
+    v[2] = static_cast<double>(uniq);
+    v[3] = static_cast<double>(resid);
+    v[4] = static_cast<double>(groups);
+    v[5] = static_cast<double>(s.n_trace_entries);
+    v[6] = static_cast<double>(s.n_unique_entries);
+    v[7] = static_cast<double>(s.n_group_entries);
+    v[8] = static_cast<double>(s.n_terms);
+    v[9] = static_cast<double>(s.n_prods);
+    v[10] = static_cast<double>(s.q0.size());
+    v[11] = static_cast<double>(s.q1.size());
+    v[12] = static_cast<double>(s.q2.size());
+    v[13] = static_cast<double>(s.n_outputs);
+    if (check_layout) {
+      // Every value index is written by exactly one entry of one distinct
+      // list; every other list reads the values of a list with its operands.
+      bool ok = true;
+      for (auto const &w : s.waves) {
+        std::vector<uint8_t> seen(static_cast<size_t>(w.n_values), 0);
+        for (int32_t l : w.unique_lists) {
+          auto const &L = w.lists[l];
+          int64_t const ne = static_cast<int64_t>(s.shapes[L.shape].i.size());
+          for (int64_t e = 0; e < ne; ++e) {
+            int64_t const k = L.val_off + e * L.stride;
+            if (k < 0 || k >= w.n_values || seen[k]++) ok = false;
+          }
+        }
+        for (auto c : seen)
+          if (c != 1) ok = false;
+        std::map<std::tuple<int32_t, int32_t, int32_t>, std::pair<int64_t, int32_t>> where;
+        for (int32_t l : w.unique_lists) {
+          auto const &L = w.lists[l];
+          where[{L.shape, L.a_base, L.b_base}] = {L.val_off, L.stride};
+        }
+        for (auto const &L : w.lists) {
+          auto it = where.find({L.shape, L.a_base, L.b_base});
+          if (it == where.end() || it->second != std::make_pair(L.val_off, L.stride)) ok = false;
+        }
+        int64_t ge = 0;
+        for (auto const &g : w.groups)
+          ge += static_cast<int64_t>(s.shapes[g.shape].i.size()) * g.n_a * g.n_b;
+        if (ge != w.n_group_entries || w.n_group_values != ge) ok = false;
+      }
+      v[14] = ok ? 1.0 : 0.0;
+    }
+    for (int32_t i = 0; i < n && i < 16; ++i) out[i] = v[i];
+  });
 }
 
 }  // extern "C"

@@ -120,6 +120,7 @@ PROTOTYPES = {
     "slaph_host_unregister": (C.c_int, [C.c_void_p]),
     "slaph_contract": (C.c_int, [C.c_void_p, C.POINTER(Plan), C.c_int, C.c_int, C.c_int, _dp]),
     "slaph_plan_output_doubles": (_i64, [C.POINTER(Plan), _i32]),
+    "slaph_plan_schedule_stats": (C.c_int, [C.c_void_p, C.c_void_p, _i32, _i32, _dp, _i32]),
     "slaph_engine_timings": (C.c_int, [C.c_void_p, _dp, C.c_int]),
     "slaph_engine_stats": (C.c_int, [C.c_void_p, _dp, C.c_int]),
 }
