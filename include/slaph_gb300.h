@@ -230,7 +230,9 @@ int slaph_engine_set_operators(slaph_engine *eng, const slaph_vdv_op *ops, int32
  * the copy asynchronous, pageable ones are copied before the call returns.
  * The reference reads each eigenvector timeslice inside the VdaggerV loop
  * (src/OperatorFactory.cpp:274-278); these calls are the device-side
- * counterpart of that overlap. */
+ * counterpart of that overlap.  slaph_contract uses the VdaggerV of the last
+ * slaph_vdaggerv_build, so the next configuration's eigenvectors may be
+ * uploaded between a build and the contraction that follows it. */
 int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V);
 int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram);
 int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise);

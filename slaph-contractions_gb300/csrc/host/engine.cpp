@@ -173,7 +173,9 @@ void Engine::set_eigenvectors(int32_t t, double const *V, bool async) {
   SLAPH_CK(cudaEventRecord(ev_v_[t], up_stream_));
   pend_v_[t] = 1;
   if (!async) SLAPH_CK(cudaEventSynchronize(ev_v_[t]));
-  vdv_built_ = false;
+  // The VdaggerV of the last build stays valid for contract(): it lives in its
+  // own buffer, so the next configuration's eigenvectors may be uploaded while
+  // this one contracts.
 }
 
 void Engine::set_perambulator(int32_t r, double const *P, bool async) {

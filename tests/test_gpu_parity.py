@@ -238,16 +238,22 @@ def test_async_uploads_match_blocking_uploads(precision):
 
     eng = Engine(gd.dims)
     eng.set_operators(gd.plan)
+    cases = [([pinned(v) for v in VV], [pinned(p) for p in PP], pinned(noise))
+             for VV, PP in ((V, peram), (V2, peram2))]
+    # Streamed as bench.py does: the next configuration's eigenvectors are
+    # enqueued after the build, while the contraction of this one runs.
     outs = []
-    for VV, PP in ((V, peram), (V2, peram2)):
-        hv, hp, hn = [pinned(v) for v in VV], [pinned(p) for p in PP], pinned(noise)
-        for t, v in enumerate(hv):
-            eng.set_eigenvectors(t, v, True)
+    for t, v in enumerate(cases[0][0]):
+        eng.set_eigenvectors(t, v, True)
+    for i, (hv, hp, hn) in enumerate(cases):
         for r, p in enumerate(hp):
             eng.set_perambulator(r, p, True)
         for r in range(hn.shape[0]):
             eng.set_random_vector(r, hn[r], True)
         eng.vdaggerv_build(precision)
+        if i + 1 < len(cases):
+            for t, v in enumerate(cases[i + 1][0]):
+                eng.set_eigenvectors(t, v, True)
         outs.append(eng.contract(gd.plan_ptr, precision, 0))
     for (VV, PP), out in zip(((V, peram), (V2, peram2)), outs):
         ref = make_engine(gd, VV, PP, noise)
