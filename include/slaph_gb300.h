@@ -240,6 +240,20 @@ int slaph_engine_set_eigenvectors_async(slaph_engine *eng, int32_t t, const doub
 int slaph_engine_set_perambulator_async(slaph_engine *eng, int32_t rnd_id, const double *peram);
 int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id, const double *noise);
 
+/* Gauge links of timeslice t for displaced operators: V3 x 3 x 9 complex
+ * doubles, link (site s, direction d = x, y, z) as a column-major 3x3 matrix at
+ * (3 s + d) 9 — the GaugeField::tslices layout (src/GaugeField.cpp:108-149)
+ * without its unused fourth direction, already smeared if the run smears
+ * (GaugeField::smearing_hyp is applied by the caller).  Sites and neighbours
+ * are those of GaugeField::init (src/GaugeField.cpp:39-98); displaced
+ * operators need a cubic spatial lattice.  A displaced VdaggerV is
+ * V_t^H D(V_t) with the displacement steps applied in the reference's in-place
+ * sweep order (displace_eigenvectors, src/OperatorFactory.cpp:33-55); the
+ * momentum of a displaced operator is not applied, as in the reference
+ * (:289-298).  Needed for every timeslice before slaph_vdaggerv_build when the
+ * operator table holds displaced operators. */
+int slaph_engine_set_gauge(slaph_engine *eng, int32_t t, const double *U);
+
 /* Page-locked host memory for the inputs, so that the set_* copies above run
  * at the full host-device link rate.  slaph_host_alloc returns driver-pinned
  * memory (cudaHostAlloc) that keeps that rate for its whole lifetime; free it

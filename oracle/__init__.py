@@ -29,6 +29,9 @@ def lib():
         L.oracle_gamma_table.argtypes = [C.POINTER(C.c_int32), _dp]
         L.oracle_vdaggerv.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(_dp),
                                       C.POINTER(C.c_int), C.c_int, _dp]
+        L.oracle_vdaggerv_gauge.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                            C.POINTER(_dp), C.POINTER(_dp), C.POINTER(C.c_int),
+                                            C.c_int, _dp]
         L.oracle_contract.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp, C.c_int,
                                       C.c_int, _dp]
         L.oracle_contract_sample.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp,
@@ -82,11 +85,13 @@ def gamma_table():
     return row, val
 
 
-def vdaggerv(dims, plan, V, ts=None, n_ops=None):
+def vdaggerv(dims, plan, V, ts=None, n_ops=None, U=None):
     """V: list of per-timeslice complex128 arrays (dim_row, nev) in Fortran
     order (or (nev, dim_row) C order).  Returns [n_ops][Lt][nev][nev] with each
     nev x nev block column-major (i.e. block[j][i] = VdV(i, j)).  n_ops limits
-    the computation to the first n_ops operators (timing samples)."""
+    the computation to the first n_ops operators (timing samples).  U: per
+    timeslice gauge links [site][dir][3x3 column-major] complex128, needed for
+    displaced operators."""
     n_ops = plan.n_vdv_ops if n_ops is None else min(int(n_ops), plan.n_vdv_ops)
     nev = dims.nev
     out = np.zeros((n_ops, dims.Lt, nev, nev), np.complex128)
@@ -96,8 +101,13 @@ def vdaggerv(dims, plan, V, ts=None, n_ops=None):
     else:
         ta = (C.c_int * len(ts))(*ts)
         tsp, nts = ta, len(ts)
-    _check(lib().oracle_vdaggerv(C.byref(dims), plan.vdv_ops, n_ops, plan.index_of_unity, ptrs,
-                                 tsp, nts, _p(out)))
+    if U is None:
+        _check(lib().oracle_vdaggerv(C.byref(dims), plan.vdv_ops, n_ops, plan.index_of_unity,
+                                     ptrs, tsp, nts, _p(out)))
+    else:
+        uptrs = (_dp * dims.Lt)(*[_p(u) if u is not None else _dp() for u in U])
+        _check(lib().oracle_vdaggerv_gauge(C.byref(dims), plan.vdv_ops, n_ops,
+                                           plan.index_of_unity, ptrs, uptrs, tsp, nts, _p(out)))
     return out
 
 

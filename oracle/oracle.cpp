@@ -821,6 +821,132 @@ int guarded(F &&f) {
   }
 }
 
+// GaugeField::init (src/GaugeField.cpp:39-98): neighbour tables of the
+// spatial index, restated with the same arguments (L1 = Lx, L2 = Ly).
+void gauge_neighbours(int L1, int L2, std::vector<int> &iup, std::vector<int> &idown) {
+  long const V3 = static_cast<long>(L1) * L1 * L2;
+  iup.assign(3 * V3, 0);
+  idown.assign(3 * V3, 0);
+  int const L0_h = L1 * L2;
+  int x0_h[3], x1_h[3], x2_h[3];
+  for (int x0 = 0; x0 < L1; ++x0) {
+    x0_h[2] = x0 * L0_h;
+    x0_h[0] = x0 - 1 < 0 ? L0_h * (L1 - 1) : (x0 - 1) * L0_h;
+    x0_h[1] = x0 + 1 == L1 ? 0 : (x0 + 1) * L0_h;
+    for (int x1 = 0; x1 < L1; ++x1) {
+      x1_h[2] = x1 * L2;
+      x1_h[0] = x1 - 1 < 0 ? L2 * (L1 - 1) : (x1 - 1) * L2;
+      x1_h[1] = x1 + 1 == L1 ? 0 : (x1 + 1) * L2;
+      for (int x2 = 0; x2 < L2; ++x2) {
+        x2_h[2] = x2;
+        x2_h[0] = x2 - 1 < 0 ? L2 - 1 : x2 - 1;
+        x2_h[1] = x2 + 1 == L2 ? 0 : x2 + 1;
+        long const i = x0_h[2] + x1_h[2] + x2_h[2];
+        iup[3 * i + 0] = x0_h[1] + x1_h[2] + x2_h[2];
+        iup[3 * i + 1] = x0_h[2] + x1_h[1] + x2_h[2];
+        iup[3 * i + 2] = x0_h[2] + x1_h[2] + x2_h[1];
+        idown[3 * i + 0] = x0_h[0] + x1_h[2] + x2_h[2];
+        idown[3 * i + 1] = x0_h[2] + x1_h[0] + x2_h[2];
+        idown[3 * i + 2] = x0_h[2] + x1_h[2] + x2_h[0];
+      }
+    }
+  }
+}
+
+// displace_eigenvectors (src/OperatorFactory.cpp:33-55) with forward_uv /
+// backward_uv (src/GaugeField.cpp:543-560): every step sweeps the sites in
+// index order and updates the eigenvector in place, so a site reads the
+// already-displaced value of a neighbour that precedes it.  U points to the
+// timeslice's links [site][dir][a + 3 b].
+void displace(Mat &res, cd const *U, slaph_vdv_op const &op, std::vector<int> const &iup,
+              std::vector<int> const &idown) {
+  long const V3 = res.r / 3;
+  for (int k = 0; k < op.n_disp; ++k) {
+    char const fb = op.disp[2 * k], axis = op.disp[2 * k + 1];
+    int const dir = axis == 'x' ? 0 : axis == 'y' ? 1 : 2;
+    for (int ev = 0; ev < res.c; ++ev) {
+      cd *v = &res.d[static_cast<size_t>(res.r) * ev];
+      for (long s = 0; s < V3; ++s) {
+        cd out[3];
+        if (fb == '>') {
+          long const up = iup[3 * s + dir];
+          cd const *u = U + (3 * s + dir) * 9;
+          for (int a = 0; a < 3; ++a) {
+            out[a] = 0;
+            for (int b = 0; b < 3; ++b) out[a] += mul(u[a + 3 * b], v[3 * up + b]);
+          }
+        } else {
+          long const dn = idown[3 * s + dir];
+          cd const *u = U + (3 * dn + dir) * 9;
+          for (int a = 0; a < 3; ++a) {
+            out[a] = 0;
+            for (int b = 0; b < 3; ++b) out[a] += mul(std::conj(u[b + 3 * a]), v[3 * dn + b]);
+          }
+        }
+        for (int a = 0; a < 3; ++a) v[3 * s + a] = out[a];
+      }
+    }
+  }
+}
+
+int vdaggerv_impl(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
+                  int index_of_unity, const double *const *V, const double *const *U,
+                  const int *ts, int n_ts, double *out) {
+  return guarded([&] {
+    check_dims(dims);
+    int const nev = dims->nev;
+    long const vol = static_cast<long>(dims->Lx) * dims->Ly * dims->Lz;
+    long const dim_row = 3 * vol;
+    bool displaced = false;
+    for (int i = 0; i < n_ops; ++i) {
+      if (ops[i].id != i) throw std::runtime_error("VdaggerV ids must be 0..n_ops-1");
+      if (ops[i].n_disp != 0 && ops[i].id != index_of_unity) displaced = true;
+    }
+    if (displaced && !U) throw std::runtime_error("displaced operators need a gauge field");
+    std::vector<int> iup, idown;
+    if (displaced) gauge_neighbours(dims->Lx, dims->Ly, iup, idown);
+    // momentum[op.id][x], src/OperatorFactory.cpp:209-215.
+    std::vector<cd> momentum(static_cast<size_t>(n_ops) * vol);
+    for (int i = 0; i < n_ops; ++i)
+      create_momentum(dims->Lx, dims->Ly, dims->Lz, ops[i].momentum, &momentum[i * vol]);
+    std::vector<int> tlist;
+    if (ts)
+      tlist.assign(ts, ts + n_ts);
+    else
+      for (int t = 0; t < dims->Lt; ++t) tlist.push_back(t);
+    size_t const blk = static_cast<size_t>(nev) * nev;
+#pragma omp parallel num_threads(oracle_threads())
+    {
+      std::vector<cd> W(static_cast<size_t>(dim_row) * nev);
+#pragma omp for schedule(dynamic)
+      for (size_t it = 0; it < tlist.size(); ++it) {
+        int const t = tlist[it];
+        cd const *Vt = reinterpret_cast<cd const *>(V[t]);
+        for (int o = 0; o < n_ops; ++o) {
+          cd *dst = reinterpret_cast<cd *>(out) + (static_cast<size_t>(o) * dims->Lt + t) * blk;
+          if (ops[o].id == index_of_unity) {
+            for (size_t i = 0; i < blk; ++i) dst[i] = 0;  // identity, :317
+            for (int i = 0; i < nev; ++i) dst[i + static_cast<size_t>(nev) * i] = 1.0;
+          } else if (ops[o].n_disp != 0) {
+            // W = D(V) (:289-290); the momentum is not applied to displaced operators
+            Mat res(static_cast<int>(dim_row), nev);
+            std::copy(Vt, Vt + dim_row * nev, res.d.begin());
+            displace(res, reinterpret_cast<cd const *>(U[t]), ops[o], iup, idown);
+            gemm_ah_b(Vt, res.d.data(), dim_row, nev, dst);  // :300
+          } else {
+            // W = diag(mom) V with mom(x) = momentum[x / 3] (:292-297)
+            cd const *mom = &momentum[ops[o].id * vol];
+            for (int j = 0; j < nev; ++j)
+              for (long x = 0; x < dim_row; ++x)
+                W[x + dim_row * j] = mul(mom[x / 3], Vt[x + dim_row * j]);
+            gemm_ah_b(Vt, W.data(), dim_row, nev, dst);  // :300
+          }
+        }
+      }
+    }
+  });
+}
+
 }  // namespace
 
 extern "C" {
@@ -847,51 +973,13 @@ void oracle_gamma_table(int32_t *row, double *value) {
 int oracle_vdaggerv(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
                     int index_of_unity, const double *const *V, const int *ts, int n_ts,
                     double *out) {
-  return guarded([&] {
-    check_dims(dims);
-    int const nev = dims->nev;
-    long const vol = static_cast<long>(dims->Lx) * dims->Ly * dims->Lz;
-    long const dim_row = 3 * vol;
-    for (int i = 0; i < n_ops; ++i) {
-      if (ops[i].id != i) throw std::runtime_error("VdaggerV ids must be 0..n_ops-1");
-      if (ops[i].n_disp != 0 && ops[i].id != index_of_unity)
-        throw std::runtime_error("displaced operators need a gauge field");
-    }
-    // momentum[op.id][x], src/OperatorFactory.cpp:209-215.
-    std::vector<cd> momentum(static_cast<size_t>(n_ops) * vol);
-    for (int i = 0; i < n_ops; ++i)
-      create_momentum(dims->Lx, dims->Ly, dims->Lz, ops[i].momentum, &momentum[i * vol]);
-    std::vector<int> tlist;
-    if (ts)
-      tlist.assign(ts, ts + n_ts);
-    else
-      for (int t = 0; t < dims->Lt; ++t) tlist.push_back(t);
-    size_t const blk = static_cast<size_t>(nev) * nev;
-    std::string err;
-#pragma omp parallel num_threads(oracle_threads())
-    {
-      std::vector<cd> W(static_cast<size_t>(dim_row) * nev);
-#pragma omp for schedule(dynamic)
-      for (size_t it = 0; it < tlist.size(); ++it) {
-        int const t = tlist[it];
-        cd const *Vt = reinterpret_cast<cd const *>(V[t]);
-        for (int o = 0; o < n_ops; ++o) {
-          cd *dst = reinterpret_cast<cd *>(out) + (static_cast<size_t>(o) * dims->Lt + t) * blk;
-          if (ops[o].id != index_of_unity) {
-            // W = diag(mom) V with mom(x) = momentum[x / 3] (:292-297)
-            cd const *mom = &momentum[ops[o].id * vol];
-            for (int j = 0; j < nev; ++j)
-              for (long x = 0; x < dim_row; ++x)
-                W[x + dim_row * j] = mul(mom[x / 3], Vt[x + dim_row * j]);
-            gemm_ah_b(Vt, W.data(), dim_row, nev, dst);  // :300
-          } else {
-            for (size_t i = 0; i < blk; ++i) dst[i] = 0;  // identity, :317
-            for (int i = 0; i < nev; ++i) dst[i + static_cast<size_t>(nev) * i] = 1.0;
-          }
-        }
-      }
-    }
-  });
+  return vdaggerv_impl(dims, ops, n_ops, index_of_unity, V, nullptr, ts, n_ts, out);
+}
+
+int oracle_vdaggerv_gauge(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
+                          int index_of_unity, const double *const *V, const double *const *U,
+                          const int *ts, int n_ts, double *out) {
+  return vdaggerv_impl(dims, ops, n_ops, index_of_unity, V, U, ts, n_ts, out);
 }
 
 int oracle_contract(const slaph_dims *dims, const slaph_plan *plan, const double *vdv,

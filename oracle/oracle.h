@@ -50,6 +50,14 @@ int oracle_vdaggerv(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
                     int index_of_unity, const double *const *V, const int *ts, int n_ts,
                     double *out);
 
+/* The same with displaced operators (src/OperatorFactory.cpp:33-55,289-290):
+ * U[t] points to the timeslice's gauge links, [site][dir x,y,z][3x3 column-
+ * major] complex (the GaugeField::tslices layout, src/GaugeField.cpp:108-149),
+ * neighbours as GaugeField::init builds them (src/GaugeField.cpp:39-98). */
+int oracle_vdaggerv_gauge(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
+                          int index_of_unity, const double *const *V, const double *const *U,
+                          const int *ts, int n_ts, double *out);
+
 /* contract() (src/Correlators.cpp:40-127) with the given VdaggerV array
  * ([n_ops][Lt][nev][nev]), perambulators peram[r] ((4 nev Lt) x
  * (Lt/dilT * dilE * 4) column-major) and noise ([n_rnd][Lt*4*nev]).

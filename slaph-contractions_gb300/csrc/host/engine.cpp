@@ -138,10 +138,15 @@ void Engine::set_operators(slaph_vdv_op const *ops, int32_t n, int32_t index_of_
   if (n < 0 || (n > 0 && !ops)) throw ArgError("invalid operator list");
   for (int32_t i = 0; i < n; ++i) {
     if (ops[i].id != i) throw ArgError("VdaggerV ids must be 0..n_ops-1 in order");
-    if (ops[i].n_disp != 0)
-      throw UnsupportedError(
-          "displaced operators (covariant derivative VdaggerV) are not supported by this "
-          "engine");
+    if (ops[i].n_disp < 0 || ops[i].n_disp > SLAPH_MAX_DISP)
+      throw ArgError("invalid displacement length");
+    for (int32_t k = 0; k < ops[i].n_disp; ++k) {
+      char const fb = ops[i].disp[2 * k], ax = ops[i].disp[2 * k + 1];
+      if ((fb != '<' && fb != '>') || (ax != 'x' && ax != 'y' && ax != 'z'))
+        throw ArgError("displacement steps are ('<' | '>', 'x' | 'y' | 'z') pairs");
+    }
+    if (ops[i].n_disp > 0 && (dims_.Lx != dims_.Ly || dims_.Lx != dims_.Lz))
+      throw UnsupportedError("displaced operators need a cubic spatial lattice");
   }
   if (index_of_unity >= n) throw ArgError("index_of_unity out of range");
   ops_.assign(ops, ops + n);
@@ -200,14 +205,39 @@ void Engine::set_random_vector(int32_t r, double const *noise, bool async) {
   if (!async) SLAPH_CK(cudaEventSynchronize(ev_n_[r]));
 }
 
+void Engine::set_gauge(int32_t t, double const *U) {
+  if (t < 0 || t >= dims_.Lt || !U) throw ArgError("invalid timeslice or null pointer");
+  if (dims_.Lx != dims_.Ly || dims_.Lx != dims_.Lz)
+    throw UnsupportedError("displaced operators need a cubic spatial lattice");
+  size_t const per = static_cast<size_t>(geo_.dim_row / 3) * 27;  // links of one timeslice
+  if (U_.size() == 0) {
+    U_.reserve(sizeof(double2) * per * dims_.Lt);
+    gauge_set_.assign(dims_.Lt, 0);
+  }
+  SLAPH_CK(cudaStreamWaitEvent(up_stream_, ev_v_used_, 0));
+  SLAPH_CK(cudaMemcpyAsync(U_.as<double2>() + per * t, U, per * sizeof(double2),
+                           cudaMemcpyHostToDevice, up_stream_));
+  SLAPH_CK(cudaStreamSynchronize(up_stream_));
+  gauge_set_[t] = 1;
+}
+
 void Engine::vdaggerv_build(int precision) {
   if (!ops_set_) throw StateError("slaph_engine_set_operators must be called first");
   if (precision != SLAPH_FP64 && precision != SLAPH_MIXED)
     throw ArgError("unknown precision mode");
   launches_ = 0;
-  std::vector<int32_t> computed;
-  for (auto const &o : ops_)
-    if (o.id != index_of_unity_) computed.push_back(o.id);
+  // Momentum operators (the GEMM paths below) and displaced operators (V^H D(V)).
+  std::vector<int32_t> computed, displaced;
+  for (auto const &o : ops_) {
+    if (o.id == index_of_unity_) continue;
+    (o.n_disp > 0 ? displaced : computed).push_back(o.id);
+  }
+  if (!displaced.empty()) {
+    bool all = gauge_set_.size() == static_cast<size_t>(dims_.Lt);
+    for (char c : gauge_set_) all = all && c;
+    if (!all)
+      throw StateError("displaced operators need slaph_engine_set_gauge for every timeslice");
+  }
   DevBuf list;
   upload(list, computed, stream_);
   int32_t const n_comp = static_cast<int32_t>(computed.size());
@@ -242,6 +272,33 @@ void Engine::vdaggerv_build(int precision) {
     launch(dev::vdaggerv_fp64(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
                               list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_, stream_),
            "vdaggerv_fp64");
+  }
+  // Displaced operators: W = D(V_t) step by step, then V_t^H W in FP64
+  // (src/OperatorFactory.cpp:289-290, 300); the momentum is not applied.
+  if (!displaced.empty()) {
+    for (auto e : ready)
+      if (e) SLAPH_CK(cudaStreamWaitEvent(stream_, e, 0));
+    size_t const n = static_cast<size_t>(geo_.dim_row) * dims_.nev;
+    size_t const per = static_cast<size_t>(geo_.dim_row / 3) * 27;
+    W_.reserve(sizeof(double2) * n);
+    upload(disp_ops_, displaced, stream_);
+    for (size_t k = 0; k < displaced.size(); ++k) {
+      slaph_vdv_op const &op = ops_[displaced[k]];
+      for (int32_t t = 0; t < dims_.Lt; ++t) {
+        SLAPH_CK(cudaMemcpyAsync(W_.as<double2>(), V_.as<double2>() + n * t, n * sizeof(double2),
+                                 cudaMemcpyDeviceToDevice, stream_));
+        for (int32_t s = 0; s < op.n_disp; ++s) {
+          char const ax = op.disp[2 * s + 1];
+          launch(dev::displace(W_.as<double2>(), U_.as<double2>() + per * t,
+                               ax == 'x' ? 0 : ax == 'y' ? 1 : 2, op.disp[2 * s] == '>' ? 1 : 0,
+                               geo_, stream_),
+                 "displace");
+        }
+        launch(dev::vdaggerv_fp64_w(vdv_.as<double2>(), V_.as<double2>(), W_.as<double2>(),
+                                    disp_ops_.as<int32_t>() + k, t, geo_, stream_),
+               "vdaggerv_fp64_w");
+      }
+    }
   }
   // V is not read after this point: later uploads may overwrite it.
   SLAPH_CK(cudaEventRecord(ev_v_used_, stream_));
@@ -866,8 +923,6 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     throw ArgError("unknown precision mode");
   if (accumulator != SLAPH_ACC_NATIVE && accumulator != SLAPH_ACC_KAHAN)
     throw ArgError("unknown accumulator");
-  if (plan->need_gaugefield)
-    throw UnsupportedError("displaced operators need a gauge field; not supported");
   if (plan->n_vdv_ops != static_cast<int32_t>(ops_.size()))
     throw ArgError("plan VdaggerV table does not match slaph_engine_set_operators");
   for (int32_t d = 0; d < plan->n_diagrams; ++d)

@@ -87,6 +87,9 @@ class Engine {
   void set_eigenvectors(int32_t t, double const *V, bool async = false);
   void set_perambulator(int32_t r, double const *peram, bool async = false);
   void set_random_vector(int32_t r, double const *noise, bool async = false);
+  // Gauge links of timeslice t, [site][dir x,y,z][3x3 column-major] complex,
+  // for displaced operators.
+  void set_gauge(int32_t t, double const *U);
   void vdaggerv_build(int precision);
   void vdaggerv_fetch(int32_t op, int32_t t, double *out);
   void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
@@ -111,6 +114,8 @@ class Engine {
 
   DevBuf V_, peram_, noise_, phase_, phase_fx_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
   std::vector<slaph_vdv_op> ops_;
+  DevBuf U_, W_, disp_ops_;  // gauge links, displaced eigenvector scratch, displaced op ids
+  std::vector<char> gauge_set_;
   int32_t index_of_unity_ = -1;
   bool ops_set_ = false, vdv_built_ = false;
   int64_t launches_ = 0;

@@ -59,6 +59,14 @@ int32_t gamma_row_host(int32_t m, int32_t c);
 int32_t gamma_phase_host(int32_t m, int32_t c);
 cudaError_t upload_gamma(cudaStream_t stream);
 
+// One displacement step of W (a copy of V_t) in place on a cubic lattice, in
+// the reference's sweep order (displace_eigenvectors,
+// src/OperatorFactory.cpp:33-55); U: the timeslice's links [site][dir][a + 3 b].
+cudaError_t displace(double2 *W, double2 const *U, int32_t dir, int32_t forward, Geometry g,
+                     cudaStream_t stream);
+// VdaggerV[2 op][t] = V_t^H W in FP64 (*op: device pointer to the operator id).
+cudaError_t vdaggerv_fp64_w(double2 *vdv, double2 const *V, double2 const *W,
+                            int32_t const *op, int32_t t, Geometry g, cudaStream_t stream);
 // exp(-i p.x) for every op: phase[op][x] (create_momenta,
 // src/OperatorFactory.cpp:64-95).  mom: [n_ops][3].
 cudaError_t momenta(double2 *phase, int32_t const *mom, int32_t n_ops, Geometry g,

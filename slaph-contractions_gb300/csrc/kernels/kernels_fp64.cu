@@ -88,10 +88,13 @@ __global__ void momenta_kernel(double2 *phase, int32_t const *mom, int32_t n_ops
 // CTA, 16 rows of V per step, 4 x 4 outputs per thread.
 constexpr int VT = 64, VK = 16;
 
+// kW: B = W (a displaced copy of V_t, one operator and timeslice per launch:
+// ops[0] is the operator, t0 the timeslice) instead of diag(phase) V_t.
+template <bool kW>
 __global__ void __launch_bounds__(256) vdv_fp64_kernel(double2 *vdv, double2 const *V,
                                                        double2 const *phase,
                                                        int32_t const *ops, int32_t t0,
-                                                       Geometry g) {
+                                                       Geometry g, double2 const *W) {
   __shared__ double2 As[VK][VT];
   __shared__ double2 Bs[VK][VT];
   int const nev = g.nev;
@@ -103,7 +106,7 @@ __global__ void __launch_bounds__(256) vdv_fp64_kernel(double2 *vdv, double2 con
   int const t = t0 + blockIdx.z;
   int const tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
   double2 const *Vt = V + static_cast<int64_t>(t) * nev * dim_row;
-  double2 const *ph = phase + static_cast<int64_t>(op) * vol;
+  double2 const *ph = kW ? nullptr : phase + static_cast<int64_t>(op) * vol;
   double2 acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
@@ -120,7 +123,9 @@ __global__ void __launch_bounds__(256) vdv_fp64_kernel(double2 *vdv, double2 con
       double2 a = make_double2(0, 0), b = make_double2(0, 0);
       if (x < dim_row) {
         if (i < nev) a = Vt[static_cast<int64_t>(i) * dim_row + x];
-        if (j < nev) b = cmul(ph[x / 3], Vt[static_cast<int64_t>(j) * dim_row + x]);
+        if (j < nev)
+          b = kW ? W[static_cast<int64_t>(j) * dim_row + x]
+                 : cmul(ph[x / 3], Vt[static_cast<int64_t>(j) * dim_row + x]);
       }
       As[xx][ii] = a;
       Bs[xx][ii] = b;
@@ -582,7 +587,93 @@ cudaError_t vdaggerv_fp64(double2 *vdv, double2 const *V, double2 const *phase,
   if (n == 0 || nt == 0) return cudaSuccess;
   int const tiles = (g.nev + VT - 1) / VT;
   dim3 grid(tiles * tiles, n, nt);
-  vdv_fp64_kernel<<<grid, 256, 0, stream>>>(vdv, V, phase, ops, t0, g);
+  vdv_fp64_kernel<false><<<grid, 256, 0, stream>>>(vdv, V, phase, ops, t0, g, nullptr);
+  return cudaGetLastError();
+}
+
+// displace_eigenvectors (src/OperatorFactory.cpp:33-55) for one step on a
+// cubic lattice: W (a copy of V_t) is updated in place line by line, each line
+// of the step's direction in increasing site index as the reference sweeps
+// it, so a site reads the already-displaced value of a preceding neighbour.
+// Forward: W(s) = U(s, d) W(s + d); backward: W(s) = U(s - d, d)^H W(s - d)
+// (forward_uv / backward_uv, src/GaugeField.cpp:543-560).  U: links of the
+// timeslice, [site][dir][a + 3 b].  One thread per (eigenvector, line).
+__global__ void displace_kernel(double2 *W, double2 const *U, int32_t dir, int32_t forward,
+                                Geometry g) {
+  int const L = g.Lx;
+  int64_t const lines = static_cast<int64_t>(L) * L;
+  int64_t const k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (k >= lines * g.nev) return;
+  int64_t const ev = k / lines, l = k % lines;
+  int64_t stride, base;
+  if (dir == 0) {
+    stride = lines;
+    base = l;
+  } else if (dir == 1) {
+    stride = L;
+    base = (l / L) * lines + (l % L);
+  } else {
+    stride = 1;
+    base = l * L;
+  }
+  double2 *col = W + ev * g.dim_row;
+  double2 carry[3];  // forward: updated first site; backward: updated previous site
+  for (int c = 0; c < L; ++c) {
+    int64_t const s = base + c * stride;
+    double2 v[3], out[3];
+    double2 const *u;
+    if (forward) {
+      int64_t const up = base + ((c + 1) % L) * stride;
+      bool const updated = c + 1 == L && c > 0;  // the wrap reads the updated first site
+#pragma unroll
+      for (int b = 0; b < 3; ++b) v[b] = updated ? carry[b] : col[3 * up + b];
+      u = U + (s * 3 + dir) * 9;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        double2 acc = make_double2(0, 0);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) cfma(acc, u[a + 3 * b], v[b]);
+        out[a] = acc;
+      }
+      if (c == 0)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) carry[a] = out[a];
+    } else {
+      int64_t const dn = base + ((c + L - 1) % L) * stride;
+#pragma unroll
+      for (int b = 0; b < 3; ++b) v[b] = c == 0 ? col[3 * dn + b] : carry[b];
+      u = U + (dn * 3 + dir) * 9;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        double2 acc = make_double2(0, 0);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          double2 const ub = u[b + 3 * a];
+          cfma(acc, make_double2(ub.x, -ub.y), v[b]);
+        }
+        out[a] = acc;
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) carry[a] = out[a];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) col[3 * s + a] = out[a];
+  }
+}
+
+cudaError_t displace(double2 *W, double2 const *U, int32_t dir, int32_t forward, Geometry g,
+                     cudaStream_t stream) {
+  if (dir < 0 || dir > 2 || g.Lx != g.Ly || g.Lx != g.Lz) return cudaErrorInvalidValue;
+  int64_t const n = static_cast<int64_t>(g.Lx) * g.Lx * g.nev;
+  displace_kernel<<<blocks_for(n, 128), 128, 0, stream>>>(W, U, dir, forward, g);
+  return cudaGetLastError();
+}
+
+cudaError_t vdaggerv_fp64_w(double2 *vdv, double2 const *V, double2 const *W,
+                            int32_t const *op, int32_t t, Geometry g, cudaStream_t stream) {
+  int const tiles = (g.nev + VT - 1) / VT;
+  vdv_fp64_kernel<true><<<dim3(tiles * tiles, 1, 1), 256, 0, stream>>>(vdv, V, nullptr, op, t,
+                                                                       g, W);
   return cudaGetLastError();
 }
 

@@ -114,6 +114,7 @@ PROTOTYPES = {
     "slaph_engine_set_random_vector_async": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_vdaggerv_build": (C.c_int, [C.c_void_p, C.c_int]),
     "slaph_vdaggerv_fetch": (C.c_int, [C.c_void_p, _i32, _i32, _dp]),
+    "slaph_engine_set_gauge": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "slaph_host_free": (C.c_int, [C.c_void_p]),
     "slaph_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),

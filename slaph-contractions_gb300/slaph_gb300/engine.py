@@ -98,6 +98,12 @@ class Engine:
               else L.lib().slaph_engine_set_random_vector)
         L.check(fn(self._h, r, L.dptr(noise)))
 
+    def set_gauge(self, t, U):
+        """Gauge links of timeslice t: complex (V3, 3, 9) with each 3x3 link
+        column-major (slaph_engine_set_gauge)."""
+        U = _c128(U)
+        L.check(L.lib().slaph_engine_set_gauge(self._h, t, L.dptr(U)))
+
     @staticmethod
     def pin(arr):
         """Page-lock a C-contiguous numpy array (slaph_host_register)."""

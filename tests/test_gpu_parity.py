@@ -323,3 +323,55 @@ def test_vdaggerv_mixed_cfg2_full_volume(oracle_lib):
     print(f"cfg2 VdaggerV vs extended precision: fp64 {e_fp64:.2e}, mixed {e_mixed:.2e}; "
           f"mixed build {ms:.1f} ms")
     assert e_mixed < REL_MIXED_VDV
+
+
+# ---------------------------------------------------------------- displaced operators
+def _random_links(rng, V3):
+    z = rng.standard_normal((V3, 3, 3, 3)) + 1j * rng.standard_normal((V3, 3, 3, 3))
+    q, r = np.linalg.qr(z)
+    d = np.diagonal(r, axis1=-2, axis2=-1)
+    u = q * (d / np.abs(d))[..., None, :]          # [site][dir][a][b], unitary
+    return np.ascontiguousarray(u.transpose(0, 1, 3, 2)).reshape(V3, 3, 9)  # column-major
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_displaced_operators_match_oracle(oracle_lib, tmp_path, precision):
+    """Displaced VdaggerV (src/OperatorFactory.cpp:33-55,289-290) with random
+    unitary links: forward, backward and two-step displacements, the VdaggerV
+    blocks and the C2c correlators of the displaced operators."""
+    from slaph_gb300 import GlobalData, synthetic
+    ops = ["g5.d0.p0,1", "g5.d>x.p0", "g5.d<y.p0", "g5.d>x|<z.p0,1"]
+    w = synthetic.Workload("disp4", Lt=4, L=4, nev=8, n_rnd=2, dilT=2, dilE=2,
+                           operators=ops,
+                           correlators=[f"C2c:Q0:Op{k}:Q0:Op{k}:P0" for k in range(len(ops))],
+                           seed=21)
+    gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+    V, peram, noise = workload_inputs(w)
+    V3 = gd.dims.Lx * gd.dims.Ly * gd.dims.Lz
+    rng = np.random.default_rng(8)
+    U = [_random_links(rng, V3) for _ in range(gd.dims.Lt)]
+    assert any(gd.plan.vdv_ops[o].n_disp > 0 for o in range(gd.plan.n_vdv_ops))
+    eng = make_engine(gd, V, peram, noise)
+    for t, u in enumerate(U):
+        eng.set_gauge(t, u)
+    eng.vdaggerv_build(precision)
+    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=U)
+    for op in range(gd.plan.n_vdv_ops):
+        for t in range(gd.dims.Lt):
+            assert rel_err(eng.vdaggerv_fetch(op, t), vdv[op, t].T) < 1e-12
+    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+                          gd.output_doubles()).reshape(-1, gd.dims.Lt)
+    out = eng.contract(gd.plan_ptr, precision, 0)
+    assert rel_err(out, ref) < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
+
+
+def test_displaced_operators_need_links(tmp_path):
+    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300._lib import SlaphError
+    w = synthetic.Workload("disp_nolinks", Lt=2, L=4, nev=4, n_rnd=2, dilT=1, dilE=2,
+                           operators=["g5.d>x.p0"], correlators=["C2c:Q0:Op0:Q0:Op0:P0"])
+    gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+    V, peram, noise = workload_inputs(w)
+    eng = make_engine(gd, V, peram, noise)
+    with pytest.raises(SlaphError, match="set_gauge"):
+        eng.vdaggerv_build(0)
