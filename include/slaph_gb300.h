@@ -196,6 +196,15 @@ int slaph_read_perambulator(const char *path, int32_t Lt, int32_t nev, int32_t d
 /* RandomVector::read_random_vector (src/RandomVector.cpp:87-113): Lt*4*nev
  * complex entries, index dirac + 4*(ev + nev*t). */
 int slaph_read_random_vector(const char *path, int64_t length, double *out);
+/* GaugeField::read_gauge_field with map_timeslice_to_eigen
+ * (src/GaugeField.cpp:108-149,762-928): the double-precision ILDG field of a
+ * LIME file, written per timeslice as [site][dir][3x3 column-major] complex
+ * with site x*Ly*Lz + y*Lz + z and the spatial directions x, y, z (the layout
+ * slaph_engine_set_gauge takes); n_dir = 4 adds the temporal link as a fourth
+ * direction.  out: Lt*Lx*Ly*Lz*n_dir*18 doubles.  Single-precision files are
+ * refused with SLAPH_ERR_UNSUPPORTED, as the reference refuses them. */
+int slaph_read_gauge_lime(const char *path, int32_t Lt, int32_t Lx, int32_t Ly, int32_t Lz,
+                          int32_t n_dir, double *out);
 
 /* ---- output: the reference HDF5 layout --------------------------------- */
 /* WriteHDF5Correlator (include/h5-wrapper.hpp:106-200,

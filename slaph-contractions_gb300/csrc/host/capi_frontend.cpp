@@ -159,6 +159,15 @@ int slaph_read_random_vector(const char *path, int64_t length, double *out) {
   });
 }
 
+int slaph_read_gauge_lime(const char *path, int32_t Lt, int32_t Lx, int32_t Ly, int32_t Lz,
+                          int32_t n_dir, double *out) {
+  return slaph::guarded([&] {
+    if (!path || !out || Lt < 1 || Lx < 1 || Ly < 1 || Lz < 1)
+      throw slaph::ArgError("invalid argument");
+    slaph::read_gauge_lime(path, Lt, Lx, Ly, Lz, n_dir, out);
+  });
+}
+
 int slaph_write_correlators_h5(const char *file_path, int32_t n_datasets,
                                const char *const *dataset_names, int32_t Lt, const double *data) {
   return slaph::guarded([&] {

@@ -64,6 +64,8 @@ void read_eigenvectors(char const *path, int64_t dim_row, int32_t nev, double *o
 void read_perambulator(char const *path, int32_t Lt, int32_t nev, int32_t dilT, int32_t dilE,
                        int32_t dilD, double *out);
 void read_random_vector(char const *path, int64_t length, double *out);
+void read_gauge_lime(char const *path, int32_t Lt, int32_t Lx, int32_t Ly, int32_t Lz,
+                     int32_t n_dir, double *out);
 void write_correlators_h5(char const *file_path, int32_t n, char const *const *names, int32_t Lt,
                           double const *data);
 

@@ -3,6 +3,8 @@
 //  slaph_read_eigenvectors    EigenVector::read_eigen_vector, src/EigenVector.cpp:35-76
 //  slaph_read_perambulator    Perambulator::read_perambulator, src/Perambulator.cpp:12-71
 //  slaph_read_random_vector   RandomVector::read_random_vector, src/RandomVector.cpp:87-113
+//  slaph_read_gauge_lime      GaugeField::read_gauge_field + map_timeslice_to_eigen,
+//                             src/GaugeField.cpp:108-149,762-928
 //  slaph_write_correlators_h5 WriteHDF5Correlator, include/h5-wrapper.hpp:106-200
 //
 // The HDF5 writer emits the same on-disk subset the reference's HDF5 C++ calls
@@ -77,6 +79,82 @@ void read_random_vector(char const *path, int64_t length, double *out) {
   std::fclose(fp);
   if (n != static_cast<size_t>(length))
     throw IoError(std::string("not all data could be read from random vector file ") + path);
+}
+
+// LIME container (records of a 144-byte big-endian header: magic 0x456789ab,
+// version, flags, data length, 128-byte type; data padded to 8 bytes) holding
+// an ILDG gauge field: "ildg-binary-data" of big-endian doubles, sites with x
+// fastest and t slowest, per site the links in direction order x, y, z, t,
+// each 3x3 complex row-major.  Written out as the reference's GaugeField keeps
+// them: per timeslice [site x Ly Lz + y Lz + z][dir][a + 3 b] (column-major
+// link), spatial directions 0..2 and, with n_dir == 4, the temporal link as
+// direction 3.
+void read_gauge_lime(char const *path, int32_t Lt, int32_t Lx, int32_t Ly, int32_t Lz,
+                     int32_t n_dir, double *out) {
+  if (n_dir != 3 && n_dir != 4) throw ArgError("n_dir must be 3 or 4");
+  FILE *fp = std::fopen(path, "rb");
+  if (!fp) throw IoError(std::string("Could not open file ") + path);
+  auto be64 = [](uint8_t const *p) {
+    uint64_t v = 0;
+    for (int i = 0; i < 8; ++i) v = (v << 8) | p[i];
+    return v;
+  };
+  int64_t const V3 = static_cast<int64_t>(Lx) * Ly * Lz;
+  int64_t const sites = V3 * Lt;
+  uint64_t const want = static_cast<uint64_t>(sites) * 72 * sizeof(double);
+  bool found = false;
+  uint64_t len = 0;
+  for (;;) {
+    uint8_t hdr[144];
+    if (std::fread(hdr, 1, 144, fp) != 144) break;
+    uint64_t const magic = (static_cast<uint64_t>(hdr[0]) << 24) | (hdr[1] << 16) |
+                           (hdr[2] << 8) | hdr[3];
+    if (magic != 0x456789abULL) {
+      std::fclose(fp);
+      throw IoError(std::string("not a LIME file: ") + path);
+    }
+    len = be64(hdr + 8);
+    std::string const type(reinterpret_cast<char const *>(hdr + 16),
+                           strnlen(reinterpret_cast<char const *>(hdr + 16), 128));
+    if (type == "ildg-binary-data") {
+      found = true;
+      break;
+    }
+    if (std::fseek(fp, static_cast<long>((len + 7) / 8 * 8), SEEK_CUR) != 0) break;
+  }
+  if (!found) {
+    std::fclose(fp);
+    throw IoError(std::string("no ildg-binary-data record found in file ") + path);
+  }
+  if (len != want) {
+    std::fclose(fp);
+    if (len == want / 2) throw UnsupportedError("Single precision read!");
+    throw IoError(std::string("Probably wrong lattice size or precision in file ") + path);
+  }
+  std::vector<uint8_t> site(72 * sizeof(double));
+  for (int64_t t = 0; t < Lt; ++t)
+    for (int64_t z = 0; z < Lz; ++z)
+      for (int64_t y = 0; y < Ly; ++y)
+        for (int64_t x = 0; x < Lx; ++x) {
+          if (std::fread(site.data(), 1, site.size(), fp) != site.size()) {
+            std::fclose(fp);
+            throw IoError(std::string("LIME read error while reading file ") + path);
+          }
+          int64_t const s = x * Ly * Lz + y * Lz + z;
+          for (int k = 0; k < 4; ++k) {  // file directions x, y, z, t
+            if (k == 3 && n_dir == 3) continue;
+            double *link = out + ((t * V3 + s) * n_dir + k) * 18;
+            for (int i = 0; i < 3; ++i)
+              for (int j = 0; j < 3; ++j)
+                for (int c = 0; c < 2; ++c) {
+                  uint64_t const bits = be64(site.data() + 8 * (((k * 3 + i) * 3 + j) * 2 + c));
+                  double v;
+                  std::memcpy(&v, &bits, sizeof v);
+                  link[2 * (i + 3 * j) + c] = v;
+                }
+          }
+        }
+  std::fclose(fp);
 }
 
 namespace {

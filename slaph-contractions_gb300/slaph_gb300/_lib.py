@@ -101,6 +101,7 @@ PROTOTYPES = {
     "slaph_read_eigenvectors": (C.c_int, [C.c_char_p, _i64, _i32, _dp]),
     "slaph_read_perambulator": (C.c_int, [C.c_char_p, _i32, _i32, _i32, _i32, _i32, _dp]),
     "slaph_read_random_vector": (C.c_int, [C.c_char_p, _i64, _dp]),
+    "slaph_read_gauge_lime": (C.c_int, [C.c_char_p, _i32, _i32, _i32, _i32, _i32, _dp]),
     "slaph_write_correlators_h5": (C.c_int, [C.c_char_p, _i32, C.POINTER(C.c_char_p), _i32,
                                              _dp]),
     "slaph_engine_create": (C.c_int, [C.POINTER(Dims), C.POINTER(C.c_void_p)]),

@@ -158,3 +158,15 @@ class GlobalData:
         if not check_layout:
             vals.pop("layout_ok")
         return vals
+
+
+def read_gauge_lime(path, Lt, Lx, Ly, Lz, n_dir=3):
+    """Gauge links of a LIME/ILDG file (slaph_read_gauge_lime): complex array
+    (Lt, Lx*Ly*Lz, n_dir, 9), each link column-major, directions x, y, z (and
+    t with n_dir = 4); [t] is what Engine.set_gauge(t, ...) takes for n_dir 3."""
+    import numpy as np
+    V3 = Lx * Ly * Lz
+    out = np.zeros((Lt, V3, n_dir, 9), np.complex128)
+    L.check(L.lib().slaph_read_gauge_lime(str(path).encode(), Lt, Lx, Ly, Lz, n_dir,
+                                          out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out

@@ -17,11 +17,14 @@ Outputs (committed):
                          noise [n_rnd][Lt*4*nev], and the raw bytes of one
                          file of each kind for the reader tests
   l4/goldens.npz         names, diagram of each name, values [n][Lt] complex
+  l4/gauge_conf.1000     gauge/conf.1000 verbatim: a LIME/ILDG double-precision
+                         4^4 gauge field whose xlf-info record states its
+                         average plaquette (the reader's known answer)
 
 The re-sort is done here with numpy, independently of the oracle and engine
 readers, so the three implementations check each other.
 
-Run:  python tests/golden/make_l4_fixtures.py [/path/to/reference]
+Run:  python tests/golden/make_l4_fixtures.py [/path/to/reference] [--only gauge]
 """
 from __future__ import annotations
 
@@ -55,10 +58,16 @@ def resort_perambulator(raw: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(m.T)
 
 
+def write_gauge(ref_root: Path):
+    base = ref_root / "tests" / "integration-L4"
+    (HERE / "l4" / "gauge_conf.1000").write_bytes((base / "gauge" / "conf.1000").read_bytes())
+
+
 def main(ref_root: Path):
     base = ref_root / "tests" / "integration-L4"
     out = HERE / "l4"
     out.mkdir(exist_ok=True)
+    write_gauge(ref_root)
     (out / "test_all.ini").write_text((base / "test_all.ini").read_text())
 
     V = np.zeros((Lt, NEV, DIM_ROW), np.complex128)
@@ -104,4 +113,9 @@ def main(ref_root: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = Path(args[0]) if args else Path("/root/reference")
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "gauge":
+        write_gauge(root)
+    else:
+        main(root)
