@@ -173,15 +173,20 @@ int slaph_frontend_dims(const slaph_frontend *fe, slaph_dims *out);
 /* Flattened lookup tables; the pointer stays valid until destroy. */
 int slaph_frontend_plan(const slaph_frontend *fe, const slaph_plan **out);
 /* Integer settings: "start_config", "end_config", "delta_config",
- * "single_time_slice_combination", "n_quarks", "nb_eigen_threads". */
+ * "single_time_slice_combination", "n_quarks", "nb_eigen_threads",
+ * "iterations" (HYP smearing steps). */
 int slaph_frontend_get_int(const slaph_frontend *fe, const char *key, int64_t *out);
+/* Floating-point settings: "alpha1", "alpha2" (HYP smearing strengths,
+ * src/global_data.cpp:127-135). */
+int slaph_frontend_get_double(const slaph_frontend *fe, const char *key, double *out);
 /* String settings: "output_path", "path_eigenvectors", "name_eigenvectors",
  * "handling_vdaggerv", "path_vdaggerv", "path_config". */
 int slaph_frontend_get_str(const slaph_frontend *fe, const char *key, char *buf, size_t len);
 /* File names for one gauge configuration (build_IO_names,
  * src/global_data_build_IO_names.cpp:76-85).  which: 0 = eigenvector prefix
  * (append "%03d" t), 1 = perambulator of random vector index, 2 = random
- * vector of index, 3 = correlator file suffix ("_cnfg%04d.h5"). */
+ * vector of index, 3 = correlator file suffix ("_cnfg%04d.h5"), 4 = gauge
+ * configuration ("<path_config>/conf.%04d", src/GaugeField.cpp:765-766). */
 int slaph_frontend_io_name(const slaph_frontend *fe, int config, int which, int index,
                            char *buf, size_t len);
 
@@ -252,8 +257,8 @@ int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id, cons
 /* Gauge links of timeslice t for displaced operators: V3 x 3 x 9 complex
  * doubles, link (site s, direction d = x, y, z) as a column-major 3x3 matrix at
  * (3 s + d) 9 — the GaugeField::tslices layout (src/GaugeField.cpp:108-149)
- * without its unused fourth direction, already smeared if the run smears
- * (GaugeField::smearing_hyp is applied by the caller).  Sites and neighbours
+ * without its unused fourth direction, unsmeared (slaph_engine_smear_gauge_hyp
+ * smears the stored links afterwards).  Sites and neighbours
  * are those of GaugeField::init (src/GaugeField.cpp:39-98); displaced
  * operators need a cubic spatial lattice.  A displaced VdaggerV is
  * V_t^H D(V_t) with the displacement steps applied in the reference's in-place
@@ -262,6 +267,20 @@ int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id, cons
  * (:289-298).  Needed for every timeslice before slaph_vdaggerv_build when the
  * operator table holds displaced operators. */
 int slaph_engine_set_gauge(slaph_engine *eng, int32_t t, const double *U);
+
+/* Replaces the smearing step of OperatorFactory::create_operators
+ * (src/OperatorFactory.cpp:253-260): GaugeField::smearing_hyp
+ * (src/GaugeField.cpp:322-427) with (alpha1, alpha2, iterations) applied on
+ * the device to the stored links of every timeslice, in place, in FP64.  The
+ * SU(3) back-projection proj_to_su3_imp (:203-210) takes (M^H M)^(-1/2) from a
+ * Jacobi eigen-decomposition, equal to the reference's Eigen matrix square
+ * root to rounding.  Needs slaph_engine_set_gauge for every timeslice first;
+ * iterations = 0 leaves the links unchanged (the reference's default). */
+int slaph_engine_smear_gauge_hyp(slaph_engine *eng, double alpha1, double alpha2,
+                                 int32_t iterations);
+/* Copy the stored (possibly smeared) links of timeslice t back to the host, in
+ * the slaph_engine_set_gauge layout. */
+int slaph_engine_gauge_fetch(slaph_engine *eng, int32_t t, double *out);
 
 /* Page-locked host memory for the inputs, so that the set_* copies above run
  * at the full host-device link rate.  slaph_host_alloc returns driver-pinned

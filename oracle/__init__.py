@@ -32,6 +32,8 @@ def lib():
         L.oracle_vdaggerv_gauge.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                             C.POINTER(_dp), C.POINTER(_dp), C.POINTER(C.c_int),
                                             C.c_int, _dp]
+        L.oracle_smear_hyp.argtypes = [C.c_void_p, C.POINTER(_dp), C.c_double, C.c_double,
+                                       C.c_int]
         L.oracle_contract.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp, C.c_int,
                                       C.c_int, _dp]
         L.oracle_contract_sample.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp,
@@ -108,6 +110,14 @@ def vdaggerv(dims, plan, V, ts=None, n_ops=None, U=None):
         uptrs = (_dp * dims.Lt)(*[_p(u) if u is not None else _dp() for u in U])
         _check(lib().oracle_vdaggerv_gauge(C.byref(dims), plan.vdv_ops, n_ops,
                                            plan.index_of_unity, ptrs, uptrs, tsp, nts, _p(out)))
+    return out
+
+
+def smear_hyp(dims, U, alpha1, alpha2, iterations):
+    """HYP-smeared copies of the per-timeslice links U[t] ([site][dir][9])."""
+    out = [np.array(u, dtype=np.complex128, order="C", copy=True) for u in U]
+    ptrs = (_dp * len(out))(*[_p(u) for u in out])
+    _check(lib().oracle_smear_hyp(C.byref(dims), ptrs, alpha1, alpha2, iterations))
     return out
 
 

@@ -889,6 +889,132 @@ void displace(Mat &res, cd const *U, slaph_vdv_op const &op, std::vector<int> co
   }
 }
 
+// ---------------------------------------------------------------- HYP smearing
+using M3 = std::array<cd, 9>;  // 3x3, element (a, b) at a + 3 b
+M3 m3_mul(M3 const &x, M3 const &y) {
+  M3 r{};
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      for (int k = 0; k < 3; ++k) r[a + 3 * b] += x[a + 3 * k] * y[k + 3 * b];
+  return r;
+}
+M3 m3_adj(M3 const &x) {
+  M3 r{};
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) r[a + 3 * b] = std::conj(x[b + 3 * a]);
+  return r;
+}
+M3 m3_axpy(M3 const &x, double ax, M3 const &y, double ay) {
+  M3 r{};
+  for (int i = 0; i < 9; ++i) r[i] = x[i] * ax + y[i] * ay;
+  return r;
+}
+cd m3_det(M3 const &m) {
+  return m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
+         m[6] * (m[1] * m[5] - m[4] * m[2]);
+}
+// H^(-1/2) of a Hermitian positive-definite 3x3 matrix from its eigen-
+// decomposition by cyclic complex Jacobi rotations (pairs (0,1), (0,2), (1,2);
+// stop when the off-diagonal norm is below 1e-16 of the diagonal's, at most
+// 30 sweeps).  Eigen's principal matrix square root used by the reference
+// equals V diag(sqrt(lambda)) V^H for such a matrix.
+M3 m3_inv_sqrt(M3 h) {
+  M3 v{};
+  v[0] = v[4] = v[8] = 1.0;
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    double off = std::norm(h[3]) + std::norm(h[6]) + std::norm(h[7]);
+    double diag = std::norm(h[0]) + std::norm(h[4]) + std::norm(h[8]);
+    if (off <= 1e-32 * diag) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        cd const apq = h[p + 3 * q];
+        double const r = std::abs(apq);
+        if (r == 0) continue;
+        cd const e = apq / r;  // phase of the element
+        double const app = h[p + 3 * p].real(), aqq = h[q + 3 * q].real();
+        double const th = (aqq - app) / (2 * r);
+        double const t = (th >= 0 ? 1.0 : -1.0) / (std::abs(th) + std::sqrt(th * th + 1));
+        double const c = 1 / std::sqrt(t * t + 1), sn = t * c;
+        M3 g{};
+        g[0] = g[4] = g[8] = 1.0;
+        g[p + 3 * p] = c;
+        g[p + 3 * q] = sn;
+        g[q + 3 * p] = -sn * std::conj(e);
+        g[q + 3 * q] = c * std::conj(e);
+        h = m3_mul(m3_adj(g), m3_mul(h, g));
+        h[p + 3 * q] = h[q + 3 * p] = 0.0;  // annihilated by the rotation
+        v = m3_mul(v, g);
+      }
+  }
+  M3 d{};
+  for (int i = 0; i < 3; ++i) d[i + 3 * i] = 1 / std::sqrt(h[i + 3 * i].real());
+  return m3_mul(v, m3_mul(d, m3_adj(v)));
+}
+// proj_to_su3_imp (src/GaugeField.cpp:203-210): M (M^H M)^(-1/2), divided by
+// the principal cube root of its determinant.
+M3 proj_su3(M3 const &m) {
+  M3 out = m3_mul(m, m3_inv_sqrt(m3_mul(m3_adj(m), m)));
+  cd const f = 1. / std::pow(m3_det(out), 1. / 3.);
+  for (auto &x : out) x *= f;
+  return out;
+}
+
+// GaugeField::smearing_hyp (src/GaugeField.cpp:322-427) on one timeslice:
+// U [site][dir][9], in place.
+void smear_hyp(cd *U, long V3, double alpha1, double alpha2, int iter,
+               std::vector<int> const &iup, std::vector<int> const &idown) {
+  auto link = [&](long s, int d) {
+    M3 m;
+    std::copy(U + (3 * s + d) * 9, U + (3 * s + d) * 9 + 9, m.begin());
+    return m;
+  };
+  static int const perp[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+  auto decor = [](int dir, int plane) {
+    if (dir == 0) return plane == 1 ? 0 : 3;
+    if (dir == 1) return plane == 0 ? 1 : 4;
+    return plane == 0 ? 2 : 5;
+  };
+  std::vector<M3> dec(static_cast<size_t>(V3) * 6), fresh(static_cast<size_t>(V3) * 3);
+  for (int run = 0; run < iter; ++run) {
+    for (long v = 0; v < V3; ++v)
+      for (int dir = 0; dir < 3; ++dir)
+        for (int n = 0; n < 2; ++n) {
+          int const pd = perp[dir][n];
+          long mu = iup[3 * v + pd];
+          long const eta = iup[3 * v + dir];
+          M3 inner = m3_mul(link(v, pd), m3_mul(link(mu, dir), m3_adj(link(eta, pd))));
+          mu = idown[3 * v + pd];
+          long const nu = iup[3 * mu + dir];
+          M3 const down = m3_mul(m3_adj(link(mu, pd)), m3_mul(link(mu, dir), link(nu, pd)));
+          for (int i = 0; i < 9; ++i) inner[i] += down[i];
+          dec[6 * v + dir + 3 * n] = proj_su3(m3_axpy(link(v, dir), 1 - alpha2, inner, alpha2 / 2.));
+        }
+    for (long i = 0; i < V3; ++i)
+      for (int dir = 0; dir < 3; ++dir) {
+        M3 outer{};
+        for (int nd = 0; nd < 3; ++nd) {
+          if (nd == dir) continue;
+          int const plane = ((dir + 1) ^ (nd + 1)) - 1;
+          long mu = iup[3 * i + nd];
+          long nu = iup[3 * mu + dir];
+          long const eta = idown[3 * nu + nd];
+          int const a = decor(nd, plane), b = decor(dir, plane);
+          M3 const up = m3_mul(dec[6 * i + a], m3_mul(dec[6 * mu + b], m3_adj(dec[6 * eta + a])));
+          mu = idown[3 * i + nd];
+          nu = iup[3 * mu + dir];
+          M3 const dn = m3_mul(m3_adj(dec[6 * mu + a]), m3_mul(dec[6 * mu + b], dec[6 * nu + a]));
+          for (int k = 0; k < 9; ++k) outer[k] += up[k] + dn[k];
+        }
+        fresh[3 * i + dir] = m3_axpy(link(i, dir), 1 - alpha1, outer, alpha1 / 4.);
+      }
+    for (long i = 0; i < V3; ++i)
+      for (int d = 0; d < 3; ++d) {
+        M3 const p = proj_su3(fresh[3 * i + d]);
+        std::copy(p.begin(), p.end(), U + (3 * i + d) * 9);
+      }
+  }
+}
+
 int vdaggerv_impl(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
                   int index_of_unity, const double *const *V, const double *const *U,
                   const int *ts, int n_ts, double *out) {
@@ -974,6 +1100,19 @@ int oracle_vdaggerv(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
                     int index_of_unity, const double *const *V, const int *ts, int n_ts,
                     double *out) {
   return vdaggerv_impl(dims, ops, n_ops, index_of_unity, V, nullptr, ts, n_ts, out);
+}
+
+int oracle_smear_hyp(const slaph_dims *dims, double *const *U, double alpha1, double alpha2,
+                     int iterations) {
+  return guarded([&] {
+    check_dims(dims);
+    long const V3 = static_cast<long>(dims->Lx) * dims->Ly * dims->Lz;
+    std::vector<int> iup, idown;
+    gauge_neighbours(dims->Lx, dims->Ly, iup, idown);
+#pragma omp parallel for num_threads(oracle_threads())
+    for (int t = 0; t < dims->Lt; ++t)
+      smear_hyp(reinterpret_cast<cd *>(U[t]), V3, alpha1, alpha2, iterations, iup, idown);
+  });
 }
 
 int oracle_vdaggerv_gauge(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,

@@ -58,6 +58,12 @@ int oracle_vdaggerv_gauge(const slaph_dims *dims, const slaph_vdv_op *ops, int n
                           int index_of_unity, const double *const *V, const double *const *U,
                           const int *ts, int n_ts, double *out);
 
+/* GaugeField::smearing_hyp (src/GaugeField.cpp:322-427) of every timeslice,
+ * in place on U[t] (layout as above), with proj_to_su3_imp (:203-210) taking
+ * (M^H M)^(-1/2) from a Jacobi eigen-decomposition. */
+int oracle_smear_hyp(const slaph_dims *dims, double *const *U, double alpha1, double alpha2,
+                     int iterations);
+
 /* contract() (src/Correlators.cpp:40-127) with the given VdaggerV array
  * ([n_ops][Lt][nev][nev]), perambulators peram[r] ((4 nev Lt) x
  * (Lt/dilT * dilE * 4) column-major) and noise ([n_rnd][Lt*4*nev]).

@@ -67,6 +67,15 @@ int slaph_engine_set_gauge(slaph_engine *eng, int32_t t, const double *U) {
   return slaph::guarded([&] { get(eng).set_gauge(t, U); });
 }
 
+int slaph_engine_smear_gauge_hyp(slaph_engine *eng, double alpha1, double alpha2,
+                                 int32_t iterations) {
+  return slaph::guarded([&] { get(eng).smear_gauge_hyp(alpha1, alpha2, iterations); });
+}
+
+int slaph_engine_gauge_fetch(slaph_engine *eng, int32_t t, double *out) {
+  return slaph::guarded([&] { get(eng).gauge_fetch(t, out); });
+}
+
 int slaph_host_alloc(size_t bytes, void **out) {
   return slaph::guarded([&] {
     if (!out || bytes == 0) throw slaph::ArgError("null output or empty size");

@@ -102,8 +102,23 @@ int slaph_frontend_get_int(const slaph_frontend *fe, const char *key, int64_t *o
       *out = static_cast<int64_t>(gd.quarks.size());
     else if (k == "nb_eigen_threads")
       *out = gd.nb_eigen_threads;
+    else if (k == "iterations")
+      *out = gd.iterations;
     else
       throw slaph::ArgError("unknown integer setting '" + k + "'");
+  });
+}
+
+int slaph_frontend_get_double(const slaph_frontend *fe, const char *key, double *out) {
+  return slaph::guarded([&] {
+    if (!fe || !key || !out) throw slaph::ArgError("null argument");
+    std::string const k = key;
+    if (k == "alpha1")
+      *out = fe->gd.alpha1;
+    else if (k == "alpha2")
+      *out = fe->gd.alpha2;
+    else
+      throw slaph::ArgError("unknown floating-point setting '" + k + "'");
   });
 }
 

@@ -221,6 +221,34 @@ void Engine::set_gauge(int32_t t, double const *U) {
   gauge_set_[t] = 1;
 }
 
+void Engine::smear_gauge_hyp(double alpha1, double alpha2, int32_t iterations) {
+  if (iterations < 0) throw ArgError("negative number of smearing iterations");
+  if (U_.size() == 0 || std::find(gauge_set_.begin(), gauge_set_.end(), 0) != gauge_set_.end())
+    throw StateError("slaph_engine_set_gauge must be called for every timeslice before smearing");
+  if (iterations == 0) return;
+  // Scratch for the decorated links of up to 256 MiB worth of timeslices.
+  size_t const per_dec = sizeof(double) * dev::hyp_scratch_doubles_per_timeslice(dims_.Lx);
+  int32_t const chunk = static_cast<int32_t>(
+      std::max<size_t>(1, std::min<size_t>(dims_.Lt, (size_t{256} << 20) / per_dec)));
+  hyp_dec_.reserve(per_dec * chunk);
+  size_t const per = static_cast<size_t>(geo_.dim_row / 3) * 27;
+  SLAPH_CK(cudaStreamWaitEvent(stream_, ev_v_used_, 0));
+  for (int32_t it = 0; it < iterations; ++it)
+    for (int32_t t0 = 0; t0 < dims_.Lt; t0 += chunk)
+      SLAPH_CK(dev::hyp_smear(U_.as<double2>() + per * t0, hyp_dec_.as<double2>(), dims_.Lx,
+                              std::min(chunk, dims_.Lt - t0), alpha1, alpha2, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+}
+
+void Engine::gauge_fetch(int32_t t, double *out) {
+  if (t < 0 || t >= dims_.Lt || !out) throw ArgError("invalid timeslice or null pointer");
+  if (U_.size() == 0 || !gauge_set_[t]) throw StateError("no gauge links for this timeslice");
+  size_t const per = static_cast<size_t>(geo_.dim_row / 3) * 27;
+  SLAPH_CK(cudaMemcpyAsync(out, U_.as<double2>() + per * t, per * sizeof(double2),
+                           cudaMemcpyDeviceToHost, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+}
+
 void Engine::vdaggerv_build(int precision) {
   if (!ops_set_) throw StateError("slaph_engine_set_operators must be called first");
   if (precision != SLAPH_FP64 && precision != SLAPH_MIXED)

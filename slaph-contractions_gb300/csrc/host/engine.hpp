@@ -90,6 +90,9 @@ class Engine {
   // Gauge links of timeslice t, [site][dir x,y,z][3x3 column-major] complex,
   // for displaced operators.
   void set_gauge(int32_t t, double const *U);
+  // HYP smearing of the stored links of every timeslice, in place.
+  void smear_gauge_hyp(double alpha1, double alpha2, int32_t iterations);
+  void gauge_fetch(int32_t t, double *out);
   void vdaggerv_build(int precision);
   void vdaggerv_fetch(int32_t op, int32_t t, double *out);
   void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
@@ -115,6 +118,7 @@ class Engine {
   DevBuf V_, peram_, noise_, phase_, phase_fx_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
   std::vector<slaph_vdv_op> ops_;
   DevBuf U_, W_, disp_ops_;  // gauge links, displaced eigenvector scratch, displaced op ids
+  DevBuf hyp_dec_;           // decorated links of a chunk of timeslices (HYP smearing)
   std::vector<char> gauge_set_;
   int32_t index_of_unity_ = -1;
   bool ops_set_ = false, vdv_built_ = false;

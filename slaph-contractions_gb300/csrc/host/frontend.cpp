@@ -765,12 +765,14 @@ std::string fmt(char const *f, ...) {
 }
 }  // namespace
 
-// src/global_data_build_IO_names.cpp:7-85.
+// src/global_data_build_IO_names.cpp:7-85; the gauge configuration as
+// GaugeField::read_gauge_field names it (src/GaugeField.cpp:765-766).
 std::string io_name(GlobalData const &gd, int config, int which, int index) {
   if (which == 0)
     return fmt("%s/%s.%04d.", gd.path_eigenvectors.c_str(), gd.name_eigenvectors.c_str(),
                config);
   if (which == 3) return fmt("_cnfg%04d.h5", config);
+  if (which == 4) return fmt("%s/conf.%04d", gd.path_config.c_str(), config);
   if (which != 1 && which != 2) throw std::runtime_error("io_name: unknown kind");
   int j = 0;
   for (auto const &q : gd.quarks) {

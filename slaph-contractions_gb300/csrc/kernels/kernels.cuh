@@ -62,6 +62,13 @@ cudaError_t upload_gamma(cudaStream_t stream);
 // One displacement step of W (a copy of V_t) in place on a cubic lattice, in
 // the reference's sweep order (displace_eigenvectors,
 // src/OperatorFactory.cpp:33-55); U: the timeslice's links [site][dir][a + 3 b].
+// One HYP smearing iteration (GaugeField::smearing_hyp, src/GaugeField.cpp:
+// 322-427) of n_t consecutive timeslices of links U ([t][site][dir][9]) of a
+// cubic L^3 lattice, in place; dec: scratch of n_t
+// hyp_scratch_doubles_per_timeslice(L) doubles (the decorated links).
+int64_t hyp_scratch_doubles_per_timeslice(int32_t L);
+cudaError_t hyp_smear(double2 *U, double2 *dec, int32_t L, int32_t n_t, double alpha1,
+                      double alpha2, cudaStream_t stream);
 cudaError_t displace(double2 *W, double2 const *U, int32_t dir, int32_t forward, Geometry g,
                      cudaStream_t stream);
 // VdaggerV[2 op][t] = V_t^H W in FP64 (*op: device pointer to the operator id).

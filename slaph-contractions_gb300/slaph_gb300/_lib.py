@@ -95,6 +95,7 @@ PROTOTYPES = {
     "slaph_frontend_dims": (C.c_int, [C.c_void_p, C.POINTER(Dims)]),
     "slaph_frontend_plan": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(Plan))]),
     "slaph_frontend_get_int": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(_i64)]),
+    "slaph_frontend_get_double": (C.c_int, [C.c_void_p, C.c_char_p, _dp]),
     "slaph_frontend_get_str": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_size_t]),
     "slaph_frontend_io_name": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_char_p,
                                          C.c_size_t]),
@@ -116,6 +117,8 @@ PROTOTYPES = {
     "slaph_vdaggerv_build": (C.c_int, [C.c_void_p, C.c_int]),
     "slaph_vdaggerv_fetch": (C.c_int, [C.c_void_p, _i32, _i32, _dp]),
     "slaph_engine_set_gauge": (C.c_int, [C.c_void_p, _i32, _dp]),
+    "slaph_engine_smear_gauge_hyp": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _i32]),
+    "slaph_engine_gauge_fetch": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "slaph_host_free": (C.c_int, [C.c_void_p]),
     "slaph_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),

@@ -104,6 +104,18 @@ class Engine:
         U = _c128(U)
         L.check(L.lib().slaph_engine_set_gauge(self._h, t, L.dptr(U)))
 
+    def smear_gauge_hyp(self, alpha1, alpha2, iterations):
+        """HYP smearing of the stored links, in place (slaph_engine_smear_gauge_hyp)."""
+        L.check(L.lib().slaph_engine_smear_gauge_hyp(self._h, float(alpha1), float(alpha2),
+                                                     int(iterations)))
+
+    def gauge_fetch(self, t):
+        """Stored links of timeslice t as complex (V3, 3, 9)."""
+        v3 = self.dims.Lx * self.dims.Ly * self.dims.Lz
+        out = np.zeros((v3, 3, 9), np.complex128)
+        L.check(L.lib().slaph_engine_gauge_fetch(self._h, t, L.dptr(out)))
+        return out
+
     @staticmethod
     def pin(arr):
         """Page-lock a C-contiguous numpy array (slaph_host_register)."""
@@ -153,6 +165,17 @@ class OperatorFactory:
         self.engine = engine
         self.gd = gd
         engine.set_operators(gd.plan)
+
+    def set_gauge_field(self, U):
+        """Links of every timeslice (U[t]: complex (V3, 3, 9)), then HYP
+        smearing with the infile's (alpha1, alpha2, iterations), as
+        create_operators does after reading the configuration
+        (src/OperatorFactory.cpp:248-260)."""
+        for t in range(self.engine.dims.Lt):
+            self.engine.set_gauge(t, U[t])
+        a1, a2, n = self.gd.hyp_parameters()
+        if n > 0:
+            self.engine.smear_gauge_hyp(a1, a2, n)
 
     def create_operators(self, precision=FP64):
         self.engine.vdaggerv_build(precision)

@@ -70,6 +70,15 @@ class GlobalData:
         L.check(L.lib().slaph_frontend_get_int(self._h, key.encode(), C.byref(v)))
         return v.value
 
+    def get_double(self, key):
+        v = C.c_double()
+        L.check(L.lib().slaph_frontend_get_double(self._h, key.encode(), C.byref(v)))
+        return v.value
+
+    def hyp_parameters(self):
+        """(alpha1, alpha2, iterations) of HYP smearing (GlobalData::hyp_parameters)."""
+        return self.get_double("alpha1"), self.get_double("alpha2"), self.get_int("iterations")
+
     def get_str(self, key):
         buf = C.create_string_buffer(4096)
         L.check(L.lib().slaph_frontend_get_str(self._h, key.encode(), buf, 4096))

@@ -46,7 +46,7 @@ class Workload:
     seed: int = 1234
     orthonormal: bool = True
     description: str = ""
-    extra: dict = field(default_factory=dict)
+    extra: dict = field(default_factory=dict)  # further global settings, e.g. alpha1
 
     @property
     def dim_row(self):
@@ -55,10 +55,11 @@ class Workload:
     def infile_text(self, start_config=1):
         lines = [f"Lt = {self.Lt}", f"Lx = {self.L}", f"Ly = {self.L}", f"Lz = {self.L}",
                  f"start_config = {start_config}", f"end_config = {start_config}",
-                 f"number_of_eigen_vec = {self.nev}", "output_path = correlators",
-                 "[quarks]",
-                 f"quark = u:{self.n_rnd}:TB:{self.dilT}:EI:{self.dilE}:DF:4:synthetic",
-                 "[operator_lists]"]
+                 f"number_of_eigen_vec = {self.nev}", "output_path = correlators"]
+        lines += [f"{k} = {v}" for k, v in self.extra.items()]
+        lines += ["[quarks]",
+                  f"quark = u:{self.n_rnd}:TB:{self.dilT}:EI:{self.dilE}:DF:4:synthetic",
+                  "[operator_lists]"]
         lines += [f"operator_list = {o}" for o in self.operators]
         lines += ["[correlator_lists]"]
         lines += [f"correlator_list = {c}" for c in self.correlators]

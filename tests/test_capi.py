@@ -37,3 +37,18 @@ def test_status_codes_and_messages_without_gpu(engine_lib):
     assert engine_lib.slaph_trace_kind_arity(7) == 6
     assert engine_lib.slaph_trace_kind_name(2) == b"trQ0Q2"
     assert engine_lib.slaph_engine_create(None, C.byref(h)) == L.SLAPH_ERR_ARG
+
+
+def test_io_names_match_the_reference_fixture_tree(l4):
+    """build_IO_names (src/global_data_build_IO_names.cpp:7-85) and the gauge
+    name of GaugeField::read_gauge_field (src/GaugeField.cpp:765-766) for the
+    L4 infile: the names of the files in the reference's L4 test tree."""
+    gd = l4["gd"]
+    assert gd.io_name(1000, 0) == "eigensystem/eigenvectors.1000."
+    assert gd.io_name(1000, 1, 0) == ("light/cnfg1000/rnd_vec_00/perambulator.rndvecnb00.u."
+                                      "TsoB0002.VsoI0002.DsoF4.TsiF0004.SsiF0064.DsiF4.CsiF3."
+                                      "smeared0.01000")
+    assert gd.io_name(1000, 2, 7) == ("strange/cnfg1000/rnd_vec_02/"
+                                      "randomvector.rndvecnb02.s.nbev0016.1000")
+    assert gd.io_name(1000, 3) == "_cnfg1000.h5"
+    assert gd.io_name(1000, 4) == "/hiskp4/gauges/quenched/wilson_b5.85_L12T24/conf.1000"

@@ -365,6 +365,106 @@ def test_displaced_operators_match_oracle(oracle_lib, tmp_path, precision):
     assert rel_err(out, ref) < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
 
 
+def _hyp_error(eng, U_ref):
+    return max(float(np.max(np.abs(eng.gauge_fetch(t) - u))) for t, u in enumerate(U_ref))
+
+
+def _fixture_links(L, Lt, seed):
+    """The reference's 4^4 configuration tiled to L^3 x Lt and gauge-transformed
+    by a random SU(3) matrix per site, so that every site differs while the
+    field stays as smooth as the original (plaquette 0.604)."""
+    from slaph_gb300.frontend import read_gauge_lime
+    from conftest import GOLDEN
+    G = read_gauge_lime(GOLDEN / "l4" / "gauge_conf.1000", 4, 4, 4, 4, 3)
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in range(Lt):
+        g = G[t % 4].reshape(4, 4, 4, 3, 3, 3).swapaxes(-1, -2)  # [x0][x1][x2][dir][a][b]
+        g = np.tile(g, (L // 4, L // 4, L // 4, 1, 1, 1))
+        z = rng.standard_normal((L, L, L, 3, 3)) + 1j * rng.standard_normal((L, L, L, 3, 3))
+        q, r = np.linalg.qr(z)
+        d = np.diagonal(r, axis1=-2, axis2=-1)
+        q = q * (d / np.abs(d))[..., None, :]
+        W = q / np.linalg.det(q)[..., None, None] ** (1 / 3)
+        for k in range(3):
+            g[..., k, :, :] = W @ g[..., k, :, :] @ np.roll(W, -1, axis=k).conj().swapaxes(-1, -2)
+        out.append(np.ascontiguousarray(g.swapaxes(-1, -2).reshape(L ** 3, 3, 9)))
+    return out
+
+
+def test_hyp_smearing_matches_oracle(oracle_lib, tmp_path):
+    """GaugeField::smearing_hyp (src/GaugeField.cpp:322-427) on the device: the
+    reference's 4^4 configuration with three iterations, and that configuration
+    tiled and gauge-transformed to 40^3 x 5, which the engine smears in two
+    chunks of timeslices.  (Random "hot" links are no test of the arithmetic:
+    their blended links are nearly singular, and two exact CPU restatements of
+    the projection already differ by 1e-10 on them.)"""
+    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300.engine import Engine
+    for L, Lt, iters in [(4, 4, 3), (40, 5, 2)]:
+        w = synthetic.Workload(f"hyp{L}", Lt=Lt, L=L, nev=4, n_rnd=2, dilT=1, dilE=2,
+                               operators=["g5.d>x.p0"], correlators=["C2c:Q0:Op0:Q0:Op0:P0"])
+        gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+        U = _fixture_links(L, Lt, seed=L)
+        eng = Engine(gd.dims)
+        for t, u in enumerate(U):
+            eng.set_gauge(t, u)
+        eng.smear_gauge_hyp(0.75, 0.6, iters)
+        err = _hyp_error(eng, oracle.smear_hyp(gd.dims, U, 0.75, 0.6, iters))
+        print(f"HYP {L}^3 x {Lt}, {iters} iterations: max |device - oracle| {err:.2e}")
+        assert err < 1e-12
+        eng.smear_gauge_hyp(0.75, 0.6, 0)  # no iterations: unchanged
+        assert _hyp_error(eng, oracle.smear_hyp(gd.dims, U, 0.75, 0.6, iters)) < 1e-12
+
+
+def test_displaced_operators_with_smeared_links_match_oracle(oracle_lib, tmp_path):
+    """create_operators with HYP parameters in the infile
+    (src/OperatorFactory.cpp:248-260): links of the reference's configuration
+    smeared on the device, then the displaced VdaggerV and correlators."""
+    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300.engine import OperatorFactory
+    from slaph_gb300.frontend import read_gauge_lime
+    from conftest import GOLDEN
+    ops = ["g5.d0.p0", "g5.d>x.p0", "g5.d<y|>z.p0"]
+    w = synthetic.Workload("disp_hyp", Lt=4, L=4, nev=8, n_rnd=2, dilT=2, dilE=2, operators=ops,
+                           correlators=[f"C2c:Q0:Op{k}:Q0:Op{k}:P0" for k in range(len(ops))],
+                           extra={"alpha1": 0.62, "alpha2": 0.62, "iterations": 3}, seed=5)
+    gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+    V, peram, noise = workload_inputs(w)
+    G = read_gauge_lime(GOLDEN / "l4" / "gauge_conf.1000", 4, 4, 4, 4, 3)
+    U = [np.ascontiguousarray(G[t]) for t in range(4)]
+    eng = make_engine(gd, V, peram, noise)
+    fac = OperatorFactory(eng, gd)
+    fac.set_gauge_field(U)
+    fac.create_operators(0)
+    S = oracle.smear_hyp(gd.dims, U, 0.62, 0.62, 3)
+    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=S)
+    for op in range(gd.plan.n_vdv_ops):
+        for t in range(gd.dims.Lt):
+            assert rel_err(fac.return_vdaggerv(op, t), vdv[op, t].T) < 1e-12
+    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+                          gd.output_doubles()).reshape(-1, gd.dims.Lt)
+    assert rel_err(eng.contract(gd.plan_ptr, 0, 0), ref) < REL_FP64
+
+
+def test_smearing_needs_links(tmp_path):
+    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300._lib import SlaphError
+    from slaph_gb300.engine import Engine
+    w = synthetic.Workload("hyp_nolinks", Lt=2, L=4, nev=4, n_rnd=2, dilT=1, dilE=2,
+                           operators=["g5.d>x.p0"], correlators=["C2c:Q0:Op0:Q0:Op0:P0"])
+    gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+    eng = Engine(gd.dims)
+    with pytest.raises(SlaphError, match="set_gauge"):
+        eng.smear_gauge_hyp(0.5, 0.5, 1)
+    eng.set_gauge(0, _random_links(np.random.default_rng(1), 64))
+    with pytest.raises(SlaphError, match="set_gauge"):
+        eng.smear_gauge_hyp(0.5, 0.5, 1)
+    eng.set_gauge(1, _random_links(np.random.default_rng(2), 64))
+    with pytest.raises(SlaphError, match="negative"):
+        eng.smear_gauge_hyp(0.5, 0.5, -1)
+
+
 def test_displaced_operators_need_links(tmp_path):
     from slaph_gb300 import GlobalData, synthetic
     from slaph_gb300._lib import SlaphError
