@@ -399,8 +399,10 @@ __device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
 #pragma unroll
     for (int j = 0; j < kTN; ++j) hi[j] = lo[j] = 0.f;
     uint32_t const lane_addr = tmem + (static_cast<uint32_t>(32 * warp) << 16);
-    for (int c = 0; c < n_chunks; ++c) {
-      if (!mbar_wait(&acc_full, c & 1, err, 5)) break;
+    // Waits are decided warp-uniformly: the TMEM loads below must be reached by
+    // all lanes of a warp or by none.
+    auto promote = [&](int c) -> bool {
+      if (!__all_sync(0xffffffffu, mbar_wait(&acc_full, c & 1, err, 5))) return false;
       tc_fence_after();
 #pragma unroll
       for (int cb = 0; cb < kTN / 16; ++cb) {
@@ -442,7 +444,10 @@ __device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
       }
       tc_fence_before();
       mbar_arrive(&acc_empty);
-    }
+      return true;
+    };
+    for (int c = 0; c < n_chunks; ++c)
+      if (!promote(c)) break;
     // After a timeout the values are incomplete; *err makes the host discard them.
     epi(32 * warp + lane, hi, lo);
   }
