@@ -11,7 +11,8 @@
 //   v = conj(x) gives the unconjugated sum_k x_k w_k.
 // * Exact split.  Every row (column) is scaled by 2^-e (e: exponent of its
 //   largest |entry|) and cut into 6 signed slices of at most 8 bits:
-//   x = sum_p a_p 2^(-7-8(p-1)), a_p integer in [-128, 128], exact in BF16.
+//   x = sum_p a_p 2^(-7-8(p-1)), a_p integer in [-128, 128], exact in BF16
+//   (balanced base-256 digits of the 55-bit fixed-point value, digits6).
 //   47 bits are kept.
 // * FP32 accumulation.  Slice products a_p b_q (|.| <= 2^14) of the same
 //   scale level l = p + q are accumulated in one TMEM accumulator.  Over a chunk
@@ -186,21 +187,32 @@ __device__ __forceinline__ long long fixed55(double v, int e) {
   return bits < 0 ? -F : F;
 }
 
-// Small integer (|a| <= 2^22) to the BF16 bits of the same value (exact for
-// |a| <= 256): float via the 1.5 * 2^23 bias, then the upper 16 bits.
-__device__ __forceinline__ uint16_t small_int_bf16(int a) {
-  float const f = __int_as_float(0x4B400000 + a) - 12582912.0f;
-  return static_cast<uint16_t>(__float_as_uint(f) >> 16);
+// The 6 balanced base-256 digits of a 64-bit fixed-point value F (|F| <= 2^55)
+// at 2^48, 2^40, ..., 2^8, as floats: F = sum_p d_p 2^(48-8p) + r with
+// |r| <= 2^7, d_0 in [-128, 128] and d_1..d_5 in [-128, 127] (all exact in
+// BF16).  With G = F + C, C = 0x808080808080 (2^7 in every byte below the
+// top), the lower digits are the bytes 5..1 of G minus 128 and the top digit is
+// G >> 48: the sum of the digits is G - C + 2^7 - (G mod 2^8).  Each lower
+// digit is one byte permutation into the mantissa of 2^23 and one FP32
+// subtraction.
+__device__ __forceinline__ void digits6(long long F, float (&d)[kSlices]) {
+  long long const G = F + 0x808080808080LL;
+  uint32_t const lo = static_cast<uint32_t>(G);
+  uint32_t const hi = static_cast<uint32_t>(static_cast<unsigned long long>(G) >> 32);
+  float const bias = 8388736.0f;  // 2^23 + 128
+  d[0] = static_cast<float>(static_cast<int>(G >> 48));
+  d[1] = __int_as_float(__byte_perm(hi, 0x4B000000u, 0x7441)) - bias;
+  d[2] = __int_as_float(__byte_perm(hi, 0x4B000000u, 0x7440)) - bias;
+  d[3] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7443)) - bias;
+  d[4] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7442)) - bias;
+  d[5] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7441)) - bias;
 }
 
-__device__ __forceinline__ void slice6(long long F, uint16_t (&out)[kSlices]) {
-#pragma unroll
-  for (int p = 0; p < kSlices; ++p) {
-    int const sh = 48 - 8 * p;
-    long long const a = (F + (1LL << (sh - 1))) >> sh;
-    F -= a << sh;
-    out[p] = small_int_bf16(static_cast<int>(a));
-  }
+// Two small integers held exactly in floats to a BF16 pair (a in the low half).
+__device__ __forceinline__ uint32_t bf16x2(float a, float b) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  return r;
 }
 
 // The same for a float, with integer operations only: round(v 2^(55-e)) for
@@ -239,13 +251,12 @@ __device__ __forceinline__ int expo_of_absbits64(unsigned long long b) {
 // Writes the slices of complex element x = (fr, fi) 2^(e-55) (K index m,
 // K' = 2m, 2m+1) of A row `row` of a tile stream laid out
 // [m_tile][k_tile][slice][kTM x kTK]: row 2r gets (Re x, Im x), row 2r+1 gets
-// (-Im x, Re x).
+// (-Im x, Re x) (the negated digits of Im x).
 __device__ __forceinline__ void put_a_fx(uint8_t *region, int64_t k_tiles, int row, int64_t m,
                                          long long fr, long long fi) {
-  uint16_t sre[kSlices], sim[kSlices], snim[kSlices];
-  slice6(fr, sre);
-  slice6(fi, sim);
-  slice6(-fi, snim);
+  float dre[kSlices], dim[kSlices];
+  digits6(fr, dre);
+  digits6(fi, dim);
   int const mt = row / (kTM / 2), r0 = 2 * (row % (kTM / 2));
   int64_t const kt = m / (kTK / 2);
   int const k = 2 * static_cast<int>(m % (kTK / 2));
@@ -253,10 +264,8 @@ __device__ __forceinline__ void put_a_fx(uint8_t *region, int64_t k_tiles, int r
 #pragma unroll
   for (int p = 0; p < kSlices; ++p) {
     uint8_t *b = blk + p * kABlk;
-    *reinterpret_cast<uint32_t *>(b + core_off(r0, k)) =
-        static_cast<uint32_t>(sre[p]) | (static_cast<uint32_t>(sim[p]) << 16);
-    *reinterpret_cast<uint32_t *>(b + core_off(r0 + 1, k)) =
-        static_cast<uint32_t>(snim[p]) | (static_cast<uint32_t>(sre[p]) << 16);
+    *reinterpret_cast<uint32_t *>(b + core_off(r0, k)) = bf16x2(dre[p], dim[p]);
+    *reinterpret_cast<uint32_t *>(b + core_off(r0 + 1, k)) = bf16x2(-dim[p], dre[p]);
   }
 }
 
@@ -264,17 +273,16 @@ __device__ __forceinline__ void put_a_fx(uint8_t *region, int64_t k_tiles, int r
 // (Re y, Im y).
 __device__ __forceinline__ void put_b_fx(uint8_t *region, int64_t k_tiles, int col, int64_t m,
                                          long long fr, long long fi) {
-  uint16_t sre[kSlices], sim[kSlices];
-  slice6(fr, sre);
-  slice6(fi, sim);
+  float dre[kSlices], dim[kSlices];
+  digits6(fr, dre);
+  digits6(fi, dim);
   int const nt = col / kTN, r = col % kTN;
   int64_t const kt = m / (kTK / 2);
   int const k = 2 * static_cast<int>(m % (kTK / 2));
   uint8_t *blk = region + (static_cast<int64_t>(nt) * k_tiles + kt) * kStageB;
 #pragma unroll
   for (int p = 0; p < kSlices; ++p)
-    *reinterpret_cast<uint32_t *>(blk + p * kBBlk + core_off(r, k)) =
-        static_cast<uint32_t>(sre[p]) | (static_cast<uint32_t>(sim[p]) << 16);
+    *reinterpret_cast<uint32_t *>(blk + p * kBBlk + core_off(r, k)) = bf16x2(dre[p], dim[p]);
 }
 
 __device__ __forceinline__ void put_a(uint8_t *region, int64_t k_tiles, int row, int64_t m,

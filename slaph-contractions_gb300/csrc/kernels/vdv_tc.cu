@@ -61,29 +61,65 @@ __global__ void slice_a_kernel(uint16_t *out, double2 const *Vt, int32_t const *
   put_a(reinterpret_cast<uint8_t *>(out), k_tiles, i, x, v, expo[i]);
 }
 
-// B slices of W = diag(phase_op) V: [op][n_tile][k_tile][slice][kTN x kTK].
-// The phase product is taken in fixed point with integer operations only:
-// with V = F_v 2^(e-55) and phase = P 2^-62 (|P| <= 2^62),
+// B slices of W = diag(phase_op) V for all operators of the call:
+// [op][n_tile][k_tile][slice][kTN x kTK].  A warp covers one 8-column row
+// group of one k-tile: lane (r, kg) = (lane % 8, lane / 8) takes column
+// 8 rg + r and the 4 complex K entries 4 kg .. 4 kg + 3, i.e. one 16-byte row of
+// core matrix (rg, kg), so that each slice store of the warp writes 512
+// contiguous bytes.  V is read and put in fixed point once for all operators;
+// the phase product is taken in fixed point with integer operations only: with
+// V = F_v 2^(e-55) and phase = P 2^-62 (|P| <= 2^62),
 // W = ((F_v 4) P / 2^64) 2^(e-55), the high word of a 128-bit product.
-__global__ void slice_b_kernel(uint16_t *out, double2 const *Vt, longlong2 const *phase_fx,
-                               int32_t const *ops, int32_t const *expo, int32_t k_tiles,
-                               int32_t n_tiles, Geometry g) {
-  int64_t const x = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  int const j = blockIdx.y;
-  int const o = blockIdx.z;
-  if (x >= static_cast<int64_t>(k_tiles) * (kTK / 2)) return;
-  int const e = expo[j];
-  long long wr = 0, wi = 0;
-  if (x < g.dim_row) {
-    double2 const v = Vt[static_cast<int64_t>(j) * g.dim_row + x];
-    longlong2 const ph = phase_fx[static_cast<int64_t>(ops[o]) * (g.dim_row / 3) + x / 3];
-    long long const vr = fixed55(v.x, e) * 4, vi = fixed55(v.y, e) * 4;
-    wr = __mul64hi(vr, ph.x) - __mul64hi(vi, ph.y);
-    wi = __mul64hi(vr, ph.y) + __mul64hi(vi, ph.x);
+// Padding columns (j >= nev) and K entries (x >= dim_row) are written as zero.
+__global__ void __launch_bounds__(256)
+    slice_b_kernel(uint8_t *out, double2 const *Vt, longlong2 const *phase_fx,
+                   int32_t const *ops, int32_t n_ops, int32_t const *expo, int32_t k_tiles,
+                   int32_t n_tiles, Geometry g) {
+  int64_t const wid = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / 32;
+  int const lane = threadIdx.x % 32;
+  int64_t const groups = static_cast<int64_t>(n_tiles) * (kTN / 8);
+  if (wid >= groups * k_tiles) return;
+  int64_t const kt = wid / groups;
+  int const rgg = static_cast<int>(wid % groups);  // row group over all n tiles
+  int const nt = rgg / (kTN / 8), rg = rgg % (kTN / 8);
+  int const r = lane % 8, kg = lane / 8;
+  int const j = rgg * 8 + r;
+  int64_t const x0 = kt * (kTK / 2) + 4 * kg;
+  int64_t const sites = g.dim_row / 3;
+  long long vr[4], vi[4];
+  int64_t site[4];
+  int const e = j < g.nev ? expo[j] : 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int64_t const x = x0 + q;
+    bool const in = j < g.nev && x < g.dim_row;
+    double2 const v = in ? Vt[static_cast<int64_t>(j) * g.dim_row + x] : make_double2(0, 0);
+    vr[q] = fixed55(v.x, e) * 4;
+    vi[q] = fixed55(v.y, e) * 4;
+    site[q] = in ? x / 3 : 0;
   }
-  uint8_t *region = reinterpret_cast<uint8_t *>(out) +
-                    static_cast<int64_t>(o) * n_tiles * k_tiles * kStageB;
-  put_b_fx(region, k_tiles, j, x, wr, wi);
+  uint8_t *dst0 = out + (static_cast<int64_t>(nt) * k_tiles + kt) * kStageB +
+                  (rg * 4 + kg) * 128 + r * 16;
+  int64_t const op_stride = static_cast<int64_t>(n_tiles) * k_tiles * kStageB;
+  for (int o = 0; o < n_ops; ++o) {
+    longlong2 const *ph = phase_fx + static_cast<int64_t>(ops[o]) * sites;
+    uint32_t w[kSlices][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      longlong2 const p = ph[site[q]];
+      long long const wr = __mul64hi(vr[q], p.x) - __mul64hi(vi[q], p.y);
+      long long const wi = __mul64hi(vr[q], p.y) + __mul64hi(vi[q], p.x);
+      float dre[kSlices], dim[kSlices];
+      digits6(wr, dre);
+      digits6(wi, dim);
+#pragma unroll
+      for (int s = 0; s < kSlices; ++s) w[s][q] = bf16x2(dre[s], dim[s]);
+    }
+    uint8_t *dst = dst0 + o * op_stride;
+#pragma unroll
+    for (int s = 0; s < kSlices; ++s)
+      *reinterpret_cast<uint4 *>(dst + s * kBBlk) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+  }
 }
 
 __global__ void phase_fixed_kernel(longlong2 *dst, double2 const *src, int64_t n) {
@@ -200,6 +236,8 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
   if (e != cudaSuccess) return e;
   int64_t const xs = L.k_tiles * (kTK / 2);
   unsigned const xb = static_cast<unsigned>((xs + 255) / 256);
+  // slice_b_kernel: one warp per (k-tile, 8-column row group)
+  unsigned const bb = static_cast<unsigned>((L.k_tiles * L.n_tiles * (kTN / 8) * 32 + 255) / 256);
   for (int32_t tb = t0; tb < t0 + nt; tb += static_cast<int32_t>(batch)) {
     int32_t const nb = static_cast<int32_t>(std::min<int64_t>(batch, t0 + nt - tb));
     for (int32_t b = 0; b < nb; ++b) {
@@ -213,9 +251,9 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
       colmax_kernel<<<g.nev, 256, 0, stream>>>(expo, Vt, g);
       slice_a_kernel<<<dim3(xb, g.nev), 256, 0, stream>>>(
           reinterpret_cast<uint16_t *>(slot), Vt, expo, static_cast<int32_t>(L.k_tiles), g);
-      slice_b_kernel<<<dim3(xb, g.nev, n), 256, 0, stream>>>(
-          reinterpret_cast<uint16_t *>(slot + L.a_bytes), Vt, phase_fx, ops, expo,
-          static_cast<int32_t>(L.k_tiles), static_cast<int32_t>(L.n_tiles), g);
+      slice_b_kernel<<<bb, 256, 0, stream>>>(slot + L.a_bytes, Vt, phase_fx, ops, n, expo,
+                                              static_cast<int32_t>(L.k_tiles),
+                                              static_cast<int32_t>(L.n_tiles), g);
     }
     ozaki_gemm_kernel<<<dim3(static_cast<unsigned>(L.m_tiles),
                              static_cast<unsigned>(L.n_tiles),
