@@ -943,21 +943,41 @@ __global__ void __launch_bounds__(256) product_df_kernel(float4 *slots_n, float4
     Bs[k] = B[k];
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < ms; k += blockDim.x) {
-    int const i = k % eds, j = k / eds;
-    DfAcc ar{0.f, 0.f}, ai{0.f, 0.f};
+  // Thread (i, c) computes the four entries (i, jb + c + u per), u = 0..3, of
+  // each pass: one load of A(i, q) serves four multiply-adds, and the B loads
+  // of a warp (one column per warp when eds >= 32) are broadcasts.
+  int const per = blockDim.x / eds;
+  int const i = threadIdx.x % eds, c = threadIdx.x / eds;
+  if (c >= per) return;
+  for (int jb = 0; jb < eds; jb += 4 * per) {
+    DfAcc ar[4], ai[4];
+    int jj[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      ar[u] = ai[u] = DfAcc{0.f, 0.f};
+      jj[u] = min(jb + c + u * per, eds - 1);  // clamped: computed, not stored
+    }
     for (int q = 0; q < eds; ++q) {
       float4 const x = As[i + eds * q];
-      float4 const y = Bs[q + eds * j];
-      df_mac(ar, x.x, x.y, y.x, y.y);
-      df_mac(ar, -x.z, -x.w, y.z, y.w);
-      df_mac(ai, x.x, x.y, y.z, y.w);
-      df_mac(ai, x.z, x.w, y.x, y.y);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        float4 const y = Bs[q + eds * jj[u]];
+        df_mac(ar[u], x.x, x.y, y.x, y.y);
+        df_mac(ar[u], -x.z, -x.w, y.z, y.w);
+        df_mac(ai[u], x.x, x.y, y.z, y.w);
+        df_mac(ai[u], x.z, x.w, y.x, y.y);
+      }
     }
-    float const rh = ar.s + ar.c, ih = ai.s + ai.c;
-    float4 const f = make_float4(rh, ar.c - (rh - ar.s), ih, ai.c - (ih - ai.s));
-    slots_n[in.c * ms + k] = f;
-    slots_t[in.c * ms + j + static_cast<int64_t>(eds) * i] = f;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      int const j = jb + c + u * per;
+      if (j >= eds) break;
+      float const rh = ar[u].s + ar[u].c, ih = ai[u].s + ai[u].c;
+      float4 const f =
+          make_float4(rh, ar[u].c - (rh - ar[u].s), ih, ai[u].c - (ih - ai[u].s));
+      slots_n[in.c * ms + i + static_cast<int64_t>(eds) * j] = f;
+      slots_t[in.c * ms + j + static_cast<int64_t>(eds) * i] = f;
+    }
   }
 }
 
@@ -974,6 +994,7 @@ cudaError_t split_df(float4 *dst_n, float4 *dst_t, double2 const *src, int64_t n
 cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int64_t n,
                         int32_t eds, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
+  if (eds < 1 || eds > 256) return cudaErrorInvalidValue;  // one row per thread of 256
   size_t const smem = 2 * sizeof(float4) * eds * eds;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(product_df_kernel,
