@@ -304,6 +304,34 @@ int slaph_vdaggerv_build(slaph_engine *eng, int precision);
  * nev x nev column-major complex into out (2*nev*nev doubles). */
 int slaph_vdaggerv_fetch(slaph_engine *eng, int32_t op_id, int32_t t, double *out);
 
+/* VdaggerV files: the handling_vdaggerv modes of
+ * OperatorFactory::create_operators (src/OperatorFactory.cpp:507-520).
+ * "write" (:225-237, 302-312, write_vdaggerv :144-168): after a build, every
+ * operator but the unity is written per timeslice to
+ * "/<path>/cnfg%04d/operators.%04d.p_<p>.d_<d>.t_%03d" as nev x nev
+ * column-major complex doubles (the directory is created).  "read"
+ * (read_vdaggerv, :328-393): the blocks are read from
+ * "/<path>/cnfg%04d/operators.%04d.p_<p>_.t_%03d" (no displacement; not the
+ * name "write" produces).  "liuming" (read_vdaggerv_liuming, :395-490): one
+ * file "/<path>/VdaggerV.p<x>p<y>p<z>.conf%04d" holds all timeslices as
+ * row-major blocks; the file of -p is read and adjointed, else the file of +p
+ * is read as is.  <p> is the concatenation of std::to_string of the momentum
+ * components, <d> the displacement pairs ("000" for none).  After a read the
+ * unity operator and the dagger copies are set as after a build, and
+ * slaph_contract may follow.  Missing or short files give SLAPH_ERR_IO (the
+ * reference constructs the same message without throwing it). */
+#define SLAPH_VDV_FILE_WRITE 0
+#define SLAPH_VDV_FILE_READ 1
+#define SLAPH_VDV_FILE_LIUMING_MINUS 2
+#define SLAPH_VDV_FILE_LIUMING_PLUS 3
+int slaph_vdaggerv_write(slaph_engine *eng, const char *path_vdaggerv, int32_t config);
+/* liuming: 0 for the "read" mode, 1 for the "liuming" mode. */
+int slaph_vdaggerv_read(slaph_engine *eng, const char *path_vdaggerv, int32_t config,
+                        int32_t liuming);
+/* The file name of one operator (and timeslice, for kinds WRITE and READ). */
+int slaph_vdaggerv_file_name(const char *path_vdaggerv, int32_t config, const slaph_vdv_op *op,
+                             int32_t t, int32_t kind, char *buf, size_t len);
+
 /* contract() (src/Correlators.cpp:40-127, include/Correlators.hpp:41-54).
  * corr_out receives, for every diagram of plan (plan order) and every request
  * (request order), Lt complex values C[t] = sum / Lt exactly as Diagram::write

@@ -119,6 +119,15 @@ int slaph_vdaggerv_fetch(slaph_engine *eng, int32_t op_id, int32_t t, double *ou
   return slaph::guarded([&] { get(eng).vdaggerv_fetch(op_id, t, out); });
 }
 
+int slaph_vdaggerv_write(slaph_engine *eng, const char *path_vdaggerv, int32_t config) {
+  return slaph::guarded([&] { get(eng).vdaggerv_write(path_vdaggerv, config); });
+}
+
+int slaph_vdaggerv_read(slaph_engine *eng, const char *path_vdaggerv, int32_t config,
+                        int32_t liuming) {
+  return slaph::guarded([&] { get(eng).vdaggerv_read(path_vdaggerv, config, liuming); });
+}
+
 int slaph_contract(slaph_engine *eng, const slaph_plan *plan, int precision, int accumulator,
                    int single_block_pair, double *corr_out) {
   return slaph::guarded(

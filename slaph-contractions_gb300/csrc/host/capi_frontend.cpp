@@ -152,6 +152,14 @@ int slaph_frontend_io_name(const slaph_frontend *fe, int config, int which, int 
   });
 }
 
+int slaph_vdaggerv_file_name(const char *path_vdaggerv, int32_t config, const slaph_vdv_op *op,
+                             int32_t t, int32_t kind, char *buf, size_t len) {
+  return slaph::guarded([&] {
+    if (!path_vdaggerv || !op) throw slaph::ArgError("null argument");
+    copy_str(slaph::vdaggerv_file_name(path_vdaggerv, config, *op, t, kind), buf, len);
+  });
+}
+
 int slaph_read_eigenvectors(const char *path, int64_t dim_row, int32_t nev, double *out) {
   return slaph::guarded([&] {
     if (!path || !out || dim_row < 1 || nev < 1) throw slaph::ArgError("invalid argument");

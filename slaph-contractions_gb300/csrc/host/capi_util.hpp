@@ -68,5 +68,9 @@ void read_gauge_lime(char const *path, int32_t Lt, int32_t Lx, int32_t Ly, int32
                      int32_t n_dir, double *out);
 void write_correlators_h5(char const *file_path, int32_t n, char const *const *names, int32_t Lt,
                           double const *data);
+std::string vdaggerv_file_name(char const *path, int32_t config, slaph_vdv_op const &op,
+                               int32_t t, int32_t kind);
+void write_vdaggerv_file(std::string const &name, double const *block, int64_t nev);
+void read_vdaggerv_file(std::string const &name, double *out, int64_t n_doubles);
 
 }  // namespace slaph

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <array>
 #include <map>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 
@@ -348,6 +349,82 @@ void Engine::vdaggerv_build(int precision) {
       throw TimeoutError("split-precision VdaggerV: a bounded device wait gave up (stage " +
                          std::to_string(code) + ")");
   }
+  vdv_built_ = true;
+}
+
+void Engine::vdaggerv_write(char const *path, int32_t config) {
+  if (!vdv_built_) throw StateError("VdaggerV has not been built");
+  if (!path) throw ArgError("null path");
+  size_t const blk = static_cast<size_t>(dims_.nev) * dims_.nev;
+  std::vector<double2> host(blk * dims_.Lt);
+  for (auto const &op : ops_) {
+    if (op.id == index_of_unity_) continue;  // not written (src/OperatorFactory.cpp:315-318)
+    SLAPH_CK(cudaMemcpyAsync(host.data(), vdv_.as<double2>() + 2ULL * op.id * dims_.Lt * blk,
+                             host.size() * sizeof(double2), cudaMemcpyDeviceToHost, stream_));
+    SLAPH_CK(cudaStreamSynchronize(stream_));
+    for (int32_t t = 0; t < dims_.Lt; ++t)
+      write_vdaggerv_file(vdaggerv_file_name(path, config, op, t, SLAPH_VDV_FILE_WRITE),
+                          reinterpret_cast<double const *>(host.data() + blk * t), dims_.nev);
+  }
+}
+
+void Engine::vdaggerv_read(char const *path, int32_t config, int32_t liuming) {
+  if (!ops_set_) throw StateError("slaph_engine_set_operators must be called first");
+  if (!path) throw ArgError("null path");
+  size_t const blk = static_cast<size_t>(dims_.nev) * dims_.nev;
+  int32_t const nev = dims_.nev;
+  std::vector<double2> host(blk * dims_.Lt), file(blk * dims_.Lt);
+  // The previous contraction may still read the VdaggerV buffer.
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  for (auto const &op : ops_) {
+    if (op.id == index_of_unity_) continue;  // identity below
+    if (!liuming) {
+      // read_vdaggerv (src/OperatorFactory.cpp:328-393): one column-major block
+      // per timeslice.  The reference constructs but does not throw its
+      // exception for a missing file (leaving zeros); the engine raises it.
+      for (int32_t t = 0; t < dims_.Lt; ++t)
+        read_vdaggerv_file(vdaggerv_file_name(path, config, op, t, SLAPH_VDV_FILE_READ),
+                           reinterpret_cast<double *>(host.data() + blk * t),
+                           static_cast<int64_t>(2 * blk));
+    } else {
+      // read_vdaggerv_liuming (:395-490): all timeslices in one file of -p
+      // (row-major blocks, adjoint taken) or else of +p (row-major blocks).
+      std::string const minus =
+          vdaggerv_file_name(path, config, op, 0, SLAPH_VDV_FILE_LIUMING_MINUS);
+      std::string const plus =
+          vdaggerv_file_name(path, config, op, 0, SLAPH_VDV_FILE_LIUMING_PLUS);
+      bool adjoint = true;
+      std::FILE *probe = std::fopen(minus.c_str(), "rb");
+      if (!probe) {
+        adjoint = false;
+        probe = std::fopen(plus.c_str(), "rb");
+        if (!probe) throw IoError("can't open " + minus + " NOR " + plus);
+      }
+      std::fclose(probe);
+      read_vdaggerv_file(adjoint ? minus : plus, reinterpret_cast<double *>(file.data()),
+                         static_cast<int64_t>(2 * file.size()));
+      for (int32_t t = 0; t < dims_.Lt; ++t)
+        for (int32_t i = 0; i < nev; ++i)
+          for (int32_t j = 0; j < nev; ++j) {
+            // file: M(r, c) at r nev + c; stored: X(i, j) at i + nev j
+            size_t const o = blk * t;
+            double2 const v = adjoint ? file[o + static_cast<size_t>(j) * nev + i]
+                                      : file[o + static_cast<size_t>(i) * nev + j];
+            host[o + i + static_cast<size_t>(nev) * j] =
+                adjoint ? make_double2(v.x, -v.y) : v;
+          }
+    }
+    SLAPH_CK(cudaMemcpyAsync(vdv_.as<double2>() + 2ULL * op.id * dims_.Lt * blk, host.data(),
+                             host.size() * sizeof(double2), cudaMemcpyHostToDevice, stream_));
+    SLAPH_CK(cudaStreamSynchronize(stream_));
+  }
+  if (index_of_unity_ >= 0)
+    launch(dev::vdaggerv_identity(vdv_.as<double2>(), index_of_unity_, geo_, stream_),
+           "vdaggerv_identity");
+  launch(dev::vdaggerv_daggers(vdv_.as<double2>(), static_cast<int32_t>(ops_.size()), geo_,
+                               stream_),
+         "vdaggerv_daggers");
+  SLAPH_CK(cudaStreamSynchronize(stream_));
   vdv_built_ = true;
 }
 

@@ -95,6 +95,9 @@ class Engine {
   void gauge_fetch(int32_t t, double *out);
   void vdaggerv_build(int precision);
   void vdaggerv_fetch(int32_t op, int32_t t, double *out);
+  // VdaggerV files of the reference's handling_vdaggerv modes.
+  void vdaggerv_write(char const *path, int32_t config);
+  void vdaggerv_read(char const *path, int32_t config, int32_t liuming);
   void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
                 double *corr_out);
 

@@ -6,6 +6,9 @@
 //  slaph_read_gauge_lime      GaugeField::read_gauge_field + map_timeslice_to_eigen,
 //                             src/GaugeField.cpp:108-149,762-928
 //  slaph_write_correlators_h5 WriteHDF5Correlator, include/h5-wrapper.hpp:106-200
+//  slaph_vdaggerv_file_name   VdaggerV file names of OperatorFactory's "write",
+//                             "read" and "liuming" modes, src/OperatorFactory.cpp:
+//                             225-237,302-312,328-490
 //
 // The HDF5 writer emits the same on-disk subset the reference's HDF5 C++ calls
 // produce (superblock v0, one root group as a v1 B-tree of symbol-table nodes,
@@ -15,6 +18,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -432,6 +436,78 @@ void write_correlators_h5(char const *file_path, int32_t n, char const *const *n
   size_t const w = std::fwrite(o.b.data(), 1, o.b.size(), fp);
   int const rc = std::fclose(fp);
   if (w != o.b.size() || rc != 0) throw IoError(std::string("short write to ") + file_path);
+}
+
+// ---------------------------------------------------------------- VdaggerV files
+// Momentum digits as std::to_string of each component, concatenated
+// (src/OperatorFactory.cpp:306-308, 352-354).
+static std::string momentum_string(int32_t const m[3], int sign) {
+  return std::to_string(sign * m[0]) + std::to_string(sign * m[1]) + std::to_string(sign * m[2]);
+}
+
+std::string vdaggerv_file_name(char const *path, int32_t config, slaph_vdv_op const &op,
+                               int32_t t, int32_t kind) {
+  char buf[64];
+  std::string const p = path ? path : "";
+  switch (kind) {
+    case SLAPH_VDV_FILE_WRITE: {
+      // "/%s/cnfg%04d/" + "operators.%04d.p_%s.d_%s.t_%03d" (:225-226, 309-311);
+      // the displacement string is to_string(DisplacementDirection)
+      // (include/global_data_typedefs.hpp:108-117): "000" or the pairs.
+      std::string d;
+      for (int i = 0; i < op.n_disp; ++i) {
+        d.push_back(op.disp[2 * i]);
+        d.push_back(op.disp[2 * i + 1]);
+      }
+      if (op.n_disp == 0) d = "000";
+      std::snprintf(buf, sizeof buf, "/cnfg%04d/operators.%04d.p_", config, config);
+      std::string out = "/" + p + buf + momentum_string(op.momentum, 1) + ".d_" + d;
+      std::snprintf(buf, sizeof buf, ".t_%03d", t);
+      return out + buf;
+    }
+    case SLAPH_VDV_FILE_READ: {
+      // "/%s/cnfg%04d/operators.%04d" + ".p_" + momentum + "_.t_%03d" (:332-356):
+      // no displacement, and not the name the "write" mode produces.
+      std::snprintf(buf, sizeof buf, "/cnfg%04d/operators.%04d.p_", config, config);
+      std::string out = "/" + p + buf + momentum_string(op.momentum, 1);
+      std::snprintf(buf, sizeof buf, "_.t_%03d", t);
+      return out + buf;
+    }
+    case SLAPH_VDV_FILE_LIUMING_MINUS:
+    case SLAPH_VDV_FILE_LIUMING_PLUS: {
+      // "/%s/VdaggerV." + "p<x>p<y>p<z>.conf%04d", first with -p (:400-427).
+      int const sg = kind == SLAPH_VDV_FILE_LIUMING_MINUS ? -1 : 1;
+      std::string out = "/" + p + "/VdaggerV.";
+      for (int i = 0; i < 3; ++i) out += "p" + std::to_string(sg * op.momentum[i]);
+      std::snprintf(buf, sizeof buf, ".conf%04d", config);
+      return out + buf;
+    }
+    default:
+      throw ArgError("unknown VdaggerV file kind " + std::to_string(kind));
+  }
+}
+
+void write_vdaggerv_file(std::string const &name, double const *block, int64_t nev) {
+  // write_vdaggerv (src/OperatorFactory.cpp:144-168): nev x nev complex,
+  // column-major, native doubles.  The directory is created as build_vdaggerv
+  // does in "write" mode (:229-237).
+  std::filesystem::path const dir = std::filesystem::path(name).parent_path();
+  std::error_code ec;
+  if (!dir.empty()) std::filesystem::create_directories(dir, ec);
+  std::FILE *fp = std::fopen(name.c_str(), "wb");
+  if (!fp) throw IoError("Can't open " + name);
+  size_t const n = static_cast<size_t>(2 * nev * nev);
+  size_t const w = std::fwrite(block, sizeof(double), n, fp);
+  int const rc = std::fclose(fp);
+  if (w != n || rc != 0) throw IoError("Problems while write to " + name);
+}
+
+void read_vdaggerv_file(std::string const &name, double *out, int64_t n_doubles) {
+  std::FILE *fp = std::fopen(name.c_str(), "rb");
+  if (!fp) throw IoError("Can't open " + name);
+  size_t const r = std::fread(out, sizeof(double), static_cast<size_t>(n_doubles), fp);
+  std::fclose(fp);
+  if (r != static_cast<size_t>(n_doubles)) throw IoError("Problems while reading from " + name);
 }
 
 }  // namespace slaph

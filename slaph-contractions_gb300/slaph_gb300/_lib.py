@@ -116,6 +116,10 @@ PROTOTYPES = {
     "slaph_engine_set_random_vector_async": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_vdaggerv_build": (C.c_int, [C.c_void_p, C.c_int]),
     "slaph_vdaggerv_fetch": (C.c_int, [C.c_void_p, _i32, _i32, _dp]),
+    "slaph_vdaggerv_write": (C.c_int, [C.c_void_p, C.c_char_p, _i32]),
+    "slaph_vdaggerv_read": (C.c_int, [C.c_void_p, C.c_char_p, _i32, _i32]),
+    "slaph_vdaggerv_file_name": (C.c_int, [C.c_char_p, _i32, C.POINTER(VdvOp), _i32, _i32,
+                                           C.c_char_p, C.c_size_t]),
     "slaph_engine_set_gauge": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_engine_smear_gauge_hyp": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _i32]),
     "slaph_engine_gauge_fetch": (C.c_int, [C.c_void_p, _i32, _dp]),

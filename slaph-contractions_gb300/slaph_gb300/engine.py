@@ -136,6 +136,15 @@ class Engine:
         L.check(L.lib().slaph_vdaggerv_fetch(self._h, op, t, L.dptr(out)))
         return out.reshape(n, n).T.copy()
 
+    def vdaggerv_write(self, path_vdaggerv, config):
+        """Files of the last build in the reference's "write" layout (slaph_vdaggerv_write)."""
+        L.check(L.lib().slaph_vdaggerv_write(self._h, str(path_vdaggerv).encode(), int(config)))
+
+    def vdaggerv_read(self, path_vdaggerv, config, liuming=False):
+        """VdaggerV from files in the "read" or "liuming" layout (slaph_vdaggerv_read)."""
+        L.check(L.lib().slaph_vdaggerv_read(self._h, str(path_vdaggerv).encode(), int(config),
+                                            1 if liuming else 0))
+
     def contract(self, plan_ptr, precision=FP64, accumulator=NATIVE, single_block_pair=-1):
         """[total_requests, Lt] complex correlators, divided by Lt."""
         n = int(L.lib().slaph_plan_output_doubles(plan_ptr, self.dims.Lt))
@@ -177,8 +186,20 @@ class OperatorFactory:
         if n > 0:
             self.engine.smear_gauge_hyp(a1, a2, n)
 
-    def create_operators(self, precision=FP64):
-        self.engine.vdaggerv_build(precision)
+    def create_operators(self, precision=FP64, config=None):
+        """VdaggerV as the infile's handling_vdaggerv asks
+        (src/OperatorFactory.cpp:507-520): "build", "write" (build, then write
+        the files of configuration `config`), "read" or "liuming"."""
+        mode = self.gd.get_str("handling_vdaggerv")
+        path = self.gd.get_str("path_vdaggerv")
+        if mode in ("build", "write"):
+            self.engine.vdaggerv_build(precision)
+            if mode == "write":
+                self.engine.vdaggerv_write(path, config)
+        elif mode in ("read", "liuming"):
+            self.engine.vdaggerv_read(path, config, mode == "liuming")
+        else:
+            raise RuntimeError("The flag handling_vdaggerv in input file is wrong!")
 
     def return_vdaggerv(self, index, t):
         return self.engine.vdaggerv_fetch(index, t)

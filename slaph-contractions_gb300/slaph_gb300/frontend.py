@@ -169,6 +169,18 @@ class GlobalData:
         return vals
 
 
+VDV_FILE_WRITE, VDV_FILE_READ, VDV_FILE_LIUMING_MINUS, VDV_FILE_LIUMING_PLUS = 0, 1, 2, 3
+
+
+def vdaggerv_file_name(path_vdaggerv, config, op, t=0, kind=VDV_FILE_WRITE):
+    """Name of a VdaggerV file of the reference's handling_vdaggerv modes
+    (slaph_vdaggerv_file_name); op is a VdvOp of the plan."""
+    buf = C.create_string_buffer(4096)
+    L.check(L.lib().slaph_vdaggerv_file_name(str(path_vdaggerv).encode(), int(config),
+                                             C.byref(op), int(t), int(kind), buf, 4096))
+    return buf.value.decode()
+
+
 def read_gauge_lime(path, Lt, Lx, Ly, Lz, n_dir=3):
     """Gauge links of a LIME/ILDG file (slaph_read_gauge_lime): complex array
     (Lt, Lx*Ly*Lz, n_dir, 9), each link column-major, directions x, y, z (and

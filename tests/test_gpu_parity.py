@@ -475,3 +475,105 @@ def test_displaced_operators_need_links(tmp_path):
     eng = make_engine(gd, V, peram, noise)
     with pytest.raises(SlaphError, match="set_gauge"):
         eng.vdaggerv_build(0)
+
+
+# ---------------------------------------------------------------- VdaggerV files
+def _vdv_workload(tmp_path, name, ops, extra=None, Lt=4):
+    from slaph_gb300 import GlobalData, synthetic
+    w = synthetic.Workload(name, Lt=Lt, L=4, nev=8, n_rnd=2, dilT=2, dilE=2, operators=ops,
+                           correlators=[f"C2c:Q0:Op{k}:Q0:Op{k}:P0,1" for k in range(len(ops))],
+                           extra=extra or {}, seed=17)
+    gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+    assert gd.plan.n_vdv_ops > 2  # momentum operators besides the unity
+    return w, gd
+
+
+def test_vdaggerv_write_files(oracle_lib, tmp_path):
+    """The "write" mode (src/OperatorFactory.cpp:302-312, write_vdaggerv
+    :144-168): one column-major block per operator and timeslice, the unity
+    operator not written; bytes equal to the built blocks."""
+    import os
+    from slaph_gb300.frontend import vdaggerv_file_name
+    w, gd = _vdv_workload(tmp_path, "vdvw", ["g5.d0.p0,1", "g5.d>x.p0"], Lt=2)
+    V, peram, noise = workload_inputs(w)
+    eng = make_engine(gd, V, peram, noise)
+    rng = np.random.default_rng(4)
+    for t in range(gd.dims.Lt):
+        eng.set_gauge(t, _random_links(rng, 64))
+    eng.vdaggerv_build(1)
+    path = str(tmp_path / "vdv")
+    eng.vdaggerv_write(path, 12)
+    nev, written = gd.dims.nev, 0
+    for k in range(gd.plan.n_vdv_ops):
+        op = gd.plan.vdv_ops[k]
+        for t in range(gd.dims.Lt):
+            name = vdaggerv_file_name(path, 12, op, t)
+            if op.id == gd.plan.index_of_unity:
+                assert not os.path.exists(name)
+                continue
+            blk = np.fromfile(name, np.complex128).reshape(nev, nev).T
+            assert np.array_equal(blk, eng.vdaggerv_fetch(op.id, t))
+            written += 1
+    assert written == (gd.plan.n_vdv_ops - 1) * gd.dims.Lt
+    assert any(gd.plan.vdv_ops[k].n_disp > 0 for k in range(gd.plan.n_vdv_ops))
+
+
+def _oracle_blocks(gd, V):
+    return oracle.vdaggerv(gd.dims, gd.plan, V)  # [op][t] column-major blocks
+
+
+@pytest.mark.parametrize("liuming", [False, True])
+def test_vdaggerv_read_files_match_oracle(oracle_lib, tmp_path, liuming):
+    """The "read" and "liuming" modes (src/OperatorFactory.cpp:328-490) through
+    OperatorFactory.create_operators: blocks from files made of the oracle's
+    VdaggerV equal it exactly (liuming: -p files adjointed for even operators,
+    +p files as they are for odd ones), and the correlators match the oracle."""
+    import os
+    from slaph_gb300.engine import OperatorFactory
+    from slaph_gb300.frontend import (vdaggerv_file_name, VDV_FILE_READ,
+                                      VDV_FILE_LIUMING_MINUS, VDV_FILE_LIUMING_PLUS)
+    path = str(tmp_path / "cache")
+    mode = "liuming" if liuming else "read"
+    w, gd = _vdv_workload(tmp_path, "vdvr", ["g5.d0.p0,1"],
+                          extra={"handling_vdaggerv": mode, "path_vdaggerv": path})
+    V, peram, noise = workload_inputs(w)
+    vdv = _oracle_blocks(gd, V)
+    nev, Lt = gd.dims.nev, gd.dims.Lt
+    for k in range(gd.plan.n_vdv_ops):
+        op = gd.plan.vdv_ops[k]
+        if op.id == gd.plan.index_of_unity:
+            continue
+        A = [vdv[op.id, t].T for t in range(Lt)]  # A[t][i, j] = VdaggerV(i, j)
+        if not liuming:
+            for t in range(Lt):
+                name = vdaggerv_file_name(path, 5, op, t, VDV_FILE_READ)
+                os.makedirs(os.path.dirname(name), exist_ok=True)
+                np.ascontiguousarray(A[t].T).tofile(name)  # column-major
+        else:
+            minus = k % 2 == 0
+            name = vdaggerv_file_name(path, 5, op, 0,
+                                      VDV_FILE_LIUMING_MINUS if minus else VDV_FILE_LIUMING_PLUS)
+            os.makedirs(os.path.dirname(name), exist_ok=True)
+            rows = [(a.conj().T if minus else a) for a in A]  # row-major blocks
+            np.ascontiguousarray(np.stack(rows)).tofile(name)
+    assert len(os.listdir(path)) > 0
+    eng = make_engine(gd, V, peram, noise)
+    fac = OperatorFactory(eng, gd)
+    fac.create_operators(0, config=5)
+    for o in range(gd.plan.n_vdv_ops):
+        for t in range(Lt):
+            assert np.array_equal(fac.return_vdaggerv(o, t), vdv[o, t].T)
+    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+                          gd.output_doubles()).reshape(-1, Lt)
+    assert rel_err(eng.contract(gd.plan_ptr, 0, 0), ref) < REL_FP64
+
+
+def test_vdaggerv_read_missing_files(tmp_path):
+    from slaph_gb300._lib import SlaphError
+    w, gd = _vdv_workload(tmp_path, "vdvm", ["g5.d0.p0,1"], Lt=2)
+    V, peram, noise = workload_inputs(w)
+    eng = make_engine(gd, V, peram, noise)
+    with pytest.raises(SlaphError, match="Can't open"):
+        eng.vdaggerv_read(str(tmp_path / "nothing"), 1)
+    with pytest.raises(SlaphError, match="NOR"):
+        eng.vdaggerv_read(str(tmp_path / "nothing"), 1, liuming=True)
