@@ -44,8 +44,16 @@ UNIT = "s/gauge-config"
 # launch divided by its trace entries) on the 16^3x32 Nev=64 pipi case, keyed
 # by dilE; the kernel's traffic scales with its trace entries.
 NCU_TRACE_DRAM_BYTES_PER_ENTRY = {8: 2280.0}
-# The same for the tensor-core trace GEMM (DRAM bytes per dense-group entry).
-NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY = {}
+# The same for the tensor-core trace GEMM (DRAM bytes per dense-group entry):
+# the 58 trace-group launches of one 32^3x64 configuration moved 1368.2 GB for
+# 5.09e9 entries (one capture of dram__bytes_read/write.sum over the full-size
+# bench command), keyed by dilE.
+NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY = {8: 268.8}
+# DRAM bytes of the split-precision VdaggerV stage (colmax, slice_a, slice_b,
+# ozaki_gemm kernels) per computed (operator, timeslice), from the same
+# capture: 1974.3 GB for 16 operators x 64 timeslices at 32^3, Nev 220.  Keyed
+# by workload, since it depends on the lattice and Nev.
+NCU_VDV_STAGE_DRAM_BYTES_PER_UNIT = {"cfg3_32x64_pipi": 1.928e9}
 
 
 def load_peaks():
@@ -319,7 +327,10 @@ def run_engine(args):
         cands.append((stage_ms[0], {
             "kernel": "ozaki_gemm_kernel (+ slicing)", "bound": "tensor",
             "achieved": flops / (stage_ms[0] / 1e3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
-            "peak_source": f"MEASURED_PEAKS.json bf16_tflops ({note})", "traffic": None,
+            "peak_source": f"MEASURED_PEAKS.json bf16_tflops ({note})",
+            "traffic": (NCU_VDV_STAGE_DRAM_BYTES_PER_UNIT.get(args.workload, 0)
+                        * n_ops * w.Lt) or None,
+            "traffic_unit": "bytes per configuration (the stage's kernels together)",
             "fp64_equivalent_tflops": vdv_flops / (stage_ms[0] / 1e3) / 1e12,
             "work": "21 split-BF16 products x 8 nev^2 3L^3 flops per (operator, timeslice)"}))
     if ktim[6] > 0:
