@@ -268,13 +268,44 @@ void Engine::vdaggerv_build(int precision) {
       throw StateError("displaced operators need slaph_engine_set_gauge for every timeslice");
   }
   DevBuf list;
-  upload(list, computed, stream_);
   int32_t const n_comp = static_cast<int32_t>(computed.size());
+  // The split-precision build takes the displaced operators too (after the
+  // momentum ones); the FP64 build handles them separately below.
+  bool const tc_disp = precision == SLAPH_MIXED && !displaced.empty();
+  std::vector<int32_t> all = computed;
+  if (tc_disp) all.insert(all.end(), displaced.begin(), displaced.end());
+  upload(list, all, stream_);
+  int32_t const n_all = static_cast<int32_t>(all.size());
+  dev::VdvDisplaced dd{};
+  std::vector<int32_t> d_steps, d_n;
+  if (tc_disp) {
+    size_t const sites = static_cast<size_t>(geo_.dim_row / 3);
+    if (phase_unit_.size() < sites * sizeof(longlong2)) {
+      std::vector<longlong2> one(sites, make_longlong2(1LL << 62, 0));
+      upload(phase_unit_, one, stream_);
+      upload(unit_op_, std::vector<int32_t>{0}, stream_);
+    }
+    W_.reserve(sizeof(double2) * static_cast<size_t>(geo_.dim_row) * dims_.nev);
+    d_steps.assign(2 * dev::kMaxDispSteps * displaced.size(), 0);
+    for (size_t k = 0; k < displaced.size(); ++k) {
+      slaph_vdv_op const &op = ops_[displaced[k]];
+      if (op.n_disp > dev::kMaxDispSteps) throw UnsupportedError("too many displacement steps");
+      d_n.push_back(op.n_disp);
+      for (int32_t s = 0; s < op.n_disp; ++s) {
+        char const ax = op.disp[2 * s + 1];
+        d_steps[2 * (k * dev::kMaxDispSteps + s)] = ax == 'x' ? 0 : ax == 'y' ? 1 : 2;
+        d_steps[2 * (k * dev::kMaxDispSteps + s) + 1] = op.disp[2 * s] == '>' ? 1 : 0;
+      }
+    }
+    dd = dev::VdvDisplaced{static_cast<int32_t>(displaced.size()), d_n.data(), d_steps.data(),
+                           U_.as<double2>(), W_.as<double2>(), phase_unit_.as<longlong2>(),
+                           unit_op_.as<int32_t>()};
+  }
   if (precision == SLAPH_MIXED) {
     int sms = 0;
     SLAPH_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
-    int32_t const batch = dev::vdaggerv_tc_batch(geo_, std::max(n_comp, 1), sms, kTcScratchCap);
-    tc_scratch_.reserve(dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_comp, 1), batch));
+    int32_t const batch = dev::vdaggerv_tc_batch(geo_, std::max(n_all, 1), sms, kTcScratchCap);
+    tc_scratch_.reserve(dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), batch));
     err_.reserve(sizeof(int));
     SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
   }
@@ -289,12 +320,16 @@ void Engine::vdaggerv_build(int precision) {
     launch(dev::vdaggerv_tc(vdv_.as<double2>(), V_.as<double2>(), phase_fx_.as<longlong2>(),
                             list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_,
                             tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_,
-                            ready.data()),
+                            ready.data(), tc_disp ? &dd : nullptr),
            "vdaggerv_tc");
-    // three slicing kernels per timeslice, one GEMM per timeslice batch
+    // per timeslice three slicing kernels, and per displaced operator its
+    // steps, exponents and slicing; one GEMM per timeslice batch
     int64_t const per = static_cast<int64_t>(
-        tc_scratch_.size() / dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_comp, 1), 1));
-    launches_ += 3LL * dims_.Lt + (dims_.Lt + per - 1) / std::max<int64_t>(per, 1) - 1;
+        tc_scratch_.size() / dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), 1));
+    int64_t disp_launches = 0;
+    for (int32_t n : d_n) disp_launches += n + 2;
+    launches_ += (3LL + disp_launches) * dims_.Lt +
+                 (dims_.Lt + per - 1) / std::max<int64_t>(per, 1) - 1 - (n_comp > 0 ? 0 : dims_.Lt);
   } else {
     for (auto e : ready)
       if (e) SLAPH_CK(cudaStreamWaitEvent(stream_, e, 0));
@@ -302,9 +337,10 @@ void Engine::vdaggerv_build(int precision) {
                               list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_, stream_),
            "vdaggerv_fp64");
   }
-  // Displaced operators: W = D(V_t) step by step, then V_t^H W in FP64
-  // (src/OperatorFactory.cpp:289-290, 300); the momentum is not applied.
-  if (!displaced.empty()) {
+  // Displaced operators of the FP64 build: W = D(V_t) step by step, then
+  // V_t^H W in FP64 (src/OperatorFactory.cpp:289-290, 300); the momentum is
+  // not applied.
+  if (!displaced.empty() && !tc_disp) {
     for (auto e : ready)
       if (e) SLAPH_CK(cudaStreamWaitEvent(stream_, e, 0));
     size_t const n = static_cast<size_t>(geo_.dim_row) * dims_.nev;

@@ -122,6 +122,7 @@ class Engine {
   std::vector<slaph_vdv_op> ops_;
   DevBuf U_, W_, disp_ops_;  // gauge links, displaced eigenvector scratch, displaced op ids
   DevBuf hyp_dec_;           // decorated links of a chunk of timeslices (HYP smearing)
+  DevBuf phase_unit_, unit_op_;  // phase 1 per site and its operator index (displaced, mixed)
   std::vector<char> gauge_set_;
   int32_t index_of_unity_ = -1;
   bool ops_set_ = false, vdv_built_ = false;

@@ -96,10 +96,26 @@ size_t vdaggerv_tc_scratch_bytes(Geometry g, int32_t n_ops, int32_t batch);
 cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
                         cudaStream_t stream);
 int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes);
+// Displaced operators of the split-precision VdaggerV: ops[n_comp + d] is
+// V_t^H D_d(V_t), D_d the displacement steps of operator d applied in place to
+// a copy W of V_t (displace above), momentum not applied.
+constexpr int kMaxDispSteps = 8;
+struct VdvDisplaced {
+  int32_t n;                     // number of displaced operators
+  int32_t const *n_steps;        // host: steps per operator
+  int32_t const *steps;          // host: [n][kMaxDispSteps][2] (dir 0..2, forward 0/1)
+  double2 const *U;              // device: links [Lt][site][dir][9]
+  double2 *W;                    // device: nev x dim_row scratch
+  longlong2 const *unit_phase;   // device: phase 1 in fixed point (2^62, 0) per site
+  int32_t const *unit_op;        // device: {0}, the operator index into unit_phase
+};
+// ops: device list of n_comp momentum operators followed by disp->n displaced
+// ones; scratch sized by vdaggerv_tc_scratch_bytes for all of them.
 cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_fx,
-                        int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
+                        int32_t const *ops, int32_t n_comp, int32_t t0, int32_t nt, Geometry g,
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
-                        cudaEvent_t const *t_ready = nullptr);
+                        cudaEvent_t const *t_ready = nullptr,
+                        VdvDisplaced const *disp = nullptr);
 // (t_ready[t], when given and non-null: event after which timeslice t of V is
 // valid; the slicing of t waits for it on `stream`.)
 // Identity blocks for code 2*op (and 2*op+1).

@@ -129,11 +129,13 @@ __global__ void phase_fixed_kernel(longlong2 *dst, double2 const *src, int64_t n
   dst[k] = make_longlong2(__double2ll_rn(ldexp(v.x, 62)), __double2ll_rn(ldexp(v.y, 62)));
 }
 
-// Epilogue of one VdaggerV tile: D = (hi + lo) 2^(e_i + e_j - 14), rows
-// (2i, 2i+1) = (Re, Im) of VdaggerV(i, j), column-major nev x nev blocks.
+// Epilogue of one VdaggerV tile: D = (hi + lo) 2^(e_i + f_j - 14), rows
+// (2i, 2i+1) = (Re, Im) of VdaggerV(i, j), column-major nev x nev blocks; e:
+// exponents of the eigenvectors (A rows), f: those of the B columns (the same
+// for momentum operators, |phase| = 1; those of D(V) for displaced ones).
 struct VdvEpilogue {
   double *outd;
-  int32_t const *expo;
+  int32_t const *expo, *expo_col;
   int i0, j0, nev;
   __device__ __forceinline__ void operator()(int row, float const (&hi)[kTN],
                                              float const (&lo)[kTN]) const {
@@ -145,7 +147,7 @@ struct VdvEpilogue {
       int const j = j0 + jj;
       if (j < nev) {
         double const val = ldexp(static_cast<double>(hi[jj]) + static_cast<double>(lo[jj]),
-                                 ei + expo[j] - 14);
+                                 ei + expo_col[j] - 14);
         outd[2 * (i + static_cast<int64_t>(nev) * j) + (row & 1)] = val;
       }
     }
@@ -154,11 +156,13 @@ struct VdvEpilogue {
 
 // The GEMM: grid (m_tiles, n_tiles, n_ops * batch), kThreads threads.  Batch
 // slot b (timeslice t0 + b) has its own A slices, B slices and exponents at
-// stride slot_bytes in the scratch buffer.
+// stride slot_bytes in the scratch buffer: the eigenvectors' exponents, then
+// per operator o >= n_comp (displaced) the exponents of its B columns at
+// (1 + o) nev.
 __global__ void __launch_bounds__(kThreads, 1)
     ozaki_gemm_kernel(uint8_t const *scratch, size_t slot_bytes, size_t b_off, size_t e_off,
-                      double2 *vdv, int32_t const *ops, int32_t n_ops, int32_t k_tiles,
-                      int32_t n_tiles, int32_t t0, Geometry g, int *err) {
+                      double2 *vdv, int32_t const *ops, int32_t n_ops, int32_t n_comp,
+                      int32_t k_tiles, int32_t n_tiles, int32_t t0, Geometry g, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   int const mt = blockIdx.x, nt = blockIdx.y;
   int const o = blockIdx.z % n_ops, slot = blockIdx.z / n_ops;
@@ -167,10 +171,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint8_t const *a_src = sbase + static_cast<int64_t>(mt) * k_tiles * kStageA;
   uint8_t const *b_src =
       sbase + b_off + (static_cast<int64_t>(o) * n_tiles + nt) * k_tiles * kStageB;
+  int32_t const *expo = reinterpret_cast<int32_t const *>(sbase + e_off);
   VdvEpilogue epi{reinterpret_cast<double *>(vdv + (static_cast<int64_t>(2 * ops[o]) * g.Lt + t) *
                                                        g.nev * g.nev),
-                  reinterpret_cast<int32_t const *>(sbase + e_off), mt * (kTM / 2), nt * kTN,
-                  g.nev};
+                  expo, o < n_comp ? expo : expo + static_cast<int64_t>(1 + o) * g.nev,
+                  mt * (kTM / 2), nt * kTN, g.nev};
   ozaki_tile(smem, a_src, b_src, k_tiles, err, epi);
 }
 
@@ -189,7 +194,9 @@ TcLayout tc_layout(Geometry const &g, int32_t n_ops) {
   L.a_bytes = static_cast<size_t>(L.m_tiles * L.k_tiles) * kStageA;
   L.b_bytes = static_cast<size_t>(n_ops) * L.n_tiles * L.k_tiles * kStageB;
   L.e_off = L.a_bytes + L.b_bytes;
-  L.slot_bytes = (L.e_off + g.nev * sizeof(int32_t) + 1023) / 1024 * 1024;
+  // exponents: the eigenvectors', then room for one set per operator
+  L.slot_bytes =
+      (L.e_off + static_cast<size_t>(1 + n_ops) * g.nev * sizeof(int32_t) + 1023) / 1024 * 1024;
   return L;
 }
 }  // namespace
@@ -217,10 +224,15 @@ cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
 }
 
 cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_fx,
-                        int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
+                        int32_t const *ops, int32_t n_comp, int32_t t0, int32_t nt, Geometry g,
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
-                        cudaEvent_t const *t_ready) {
+                        cudaEvent_t const *t_ready, VdvDisplaced const *disp) {
+  int32_t const n_disp = disp ? disp->n : 0;
+  int32_t const n = n_comp + n_disp;
   if (n == 0 || nt == 0) return cudaSuccess;
+  if (n_disp > 0 && (!disp->n_steps || !disp->steps || !disp->U || !disp->W ||
+                     !disp->unit_phase || !disp->unit_op))
+    return cudaErrorInvalidValue;
   TcLayout const L = tc_layout(g, n);
   if (L.k_tiles > 0x7fffffffLL / kTK) return cudaErrorInvalidValue;
   int64_t const batch = static_cast<int64_t>(scratch_bytes / L.slot_bytes);
@@ -238,29 +250,52 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
   unsigned const xb = static_cast<unsigned>((xs + 255) / 256);
   // slice_b_kernel: one warp per (k-tile, 8-column row group)
   unsigned const bb = static_cast<unsigned>((L.k_tiles * L.n_tiles * (kTN / 8) * 32 + 255) / 256);
+  size_t const b_op = static_cast<size_t>(L.n_tiles * L.k_tiles) * kStageB;
+  size_t const links = static_cast<size_t>(g.dim_row / 3) * 27;  // of one timeslice
   for (int32_t tb = t0; tb < t0 + nt; tb += static_cast<int32_t>(batch)) {
     int32_t const nb = static_cast<int32_t>(std::min<int64_t>(batch, t0 + nt - tb));
     for (int32_t b = 0; b < nb; ++b) {
-      if (t_ready && t_ready[tb + b]) {
-        e = cudaStreamWaitEvent(stream, t_ready[tb + b], 0);
+      int32_t const t = tb + b;
+      if (t_ready && t_ready[t]) {
+        e = cudaStreamWaitEvent(stream, t_ready[t], 0);
         if (e != cudaSuccess) return e;
       }
-      double2 const *Vt = V + static_cast<int64_t>(tb + b) * g.nev * g.dim_row;
+      double2 const *Vt = V + static_cast<int64_t>(t) * g.nev * g.dim_row;
       uint8_t *slot = base + b * L.slot_bytes;
       int32_t *expo = reinterpret_cast<int32_t *>(slot + L.e_off);
       colmax_kernel<<<g.nev, 256, 0, stream>>>(expo, Vt, g);
       slice_a_kernel<<<dim3(xb, g.nev), 256, 0, stream>>>(
           reinterpret_cast<uint16_t *>(slot), Vt, expo, static_cast<int32_t>(L.k_tiles), g);
-      slice_b_kernel<<<bb, 256, 0, stream>>>(slot + L.a_bytes, Vt, phase_fx, ops, n, expo,
-                                              static_cast<int32_t>(L.k_tiles),
-                                              static_cast<int32_t>(L.n_tiles), g);
+      if (n_comp > 0)
+        slice_b_kernel<<<bb, 256, 0, stream>>>(slot + L.a_bytes, Vt, phase_fx, ops, n_comp, expo,
+                                                static_cast<int32_t>(L.k_tiles),
+                                                static_cast<int32_t>(L.n_tiles), g);
+      // Displaced operators: W = D(V_t) in the reference's in-place sweep
+      // order, B = W with phase 1 and W's own column exponents.
+      for (int32_t d = 0; d < n_disp; ++d) {
+        int32_t const o = n_comp + d;
+        e = cudaMemcpyAsync(disp->W, Vt, sizeof(double2) * g.nev * g.dim_row,
+                            cudaMemcpyDeviceToDevice, stream);
+        if (e != cudaSuccess) return e;
+        for (int32_t k = 0; k < disp->n_steps[d]; ++k) {
+          int32_t const *st = disp->steps + 2 * (static_cast<int64_t>(d) * kMaxDispSteps + k);
+          e = displace(disp->W, disp->U + links * t, st[0], st[1], g, stream);
+          if (e != cudaSuccess) return e;
+        }
+        int32_t *expo_w = expo + static_cast<int64_t>(1 + o) * g.nev;
+        colmax_kernel<<<g.nev, 256, 0, stream>>>(expo_w, disp->W, g);
+        slice_b_kernel<<<bb, 256, 0, stream>>>(slot + L.a_bytes + o * b_op, disp->W,
+                                                disp->unit_phase, disp->unit_op, 1, expo_w,
+                                                static_cast<int32_t>(L.k_tiles),
+                                                static_cast<int32_t>(L.n_tiles), g);
+      }
     }
     ozaki_gemm_kernel<<<dim3(static_cast<unsigned>(L.m_tiles),
                              static_cast<unsigned>(L.n_tiles),
                              static_cast<unsigned>(n * nb)),
                         kThreads, kSmemBytes, stream>>>(
-        base, L.slot_bytes, L.a_bytes, L.e_off, vdv, ops, n, static_cast<int32_t>(L.k_tiles),
-        static_cast<int32_t>(L.n_tiles), tb, g, err);
+        base, L.slot_bytes, L.a_bytes, L.e_off, vdv, ops, n, n_comp,
+        static_cast<int32_t>(L.k_tiles), static_cast<int32_t>(L.n_tiles), tb, g, err);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

@@ -417,7 +417,8 @@ def test_hyp_smearing_matches_oracle(oracle_lib, tmp_path):
         assert _hyp_error(eng, oracle.smear_hyp(gd.dims, U, 0.75, 0.6, iters)) < 1e-12
 
 
-def test_displaced_operators_with_smeared_links_match_oracle(oracle_lib, tmp_path):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_displaced_operators_with_smeared_links_match_oracle(oracle_lib, tmp_path, precision):
     """create_operators with HYP parameters in the infile
     (src/OperatorFactory.cpp:248-260): links of the reference's configuration
     smeared on the device, then the displaced VdaggerV and correlators."""
@@ -436,7 +437,7 @@ def test_displaced_operators_with_smeared_links_match_oracle(oracle_lib, tmp_pat
     eng = make_engine(gd, V, peram, noise)
     fac = OperatorFactory(eng, gd)
     fac.set_gauge_field(U)
-    fac.create_operators(0)
+    fac.create_operators(precision)
     S = oracle.smear_hyp(gd.dims, U, 0.62, 0.62, 3)
     vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=S)
     for op in range(gd.plan.n_vdv_ops):
@@ -444,7 +445,8 @@ def test_displaced_operators_with_smeared_links_match_oracle(oracle_lib, tmp_pat
             assert rel_err(fac.return_vdaggerv(op, t), vdv[op, t].T) < 1e-12
     ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
-    assert rel_err(eng.contract(gd.plan_ptr, 0, 0), ref) < REL_FP64
+    assert rel_err(eng.contract(gd.plan_ptr, precision, 0), ref) < (
+        REL_FP64 if precision == 0 else REL_MIXED_CORR)
 
 
 def test_smearing_needs_links(tmp_path):
