@@ -47,6 +47,9 @@ class Workload:
     orthonormal: bool = True
     description: str = ""
     extra: dict = field(default_factory=dict)  # further global settings, e.g. alpha1
+    # Quark lines replacing the single default one (flavours with the same
+    # dilution; n_rnd is then their total number of random vectors).
+    quark_lines: tuple = ()
 
     @property
     def dim_row(self):
@@ -57,9 +60,9 @@ class Workload:
                  f"start_config = {start_config}", f"end_config = {start_config}",
                  f"number_of_eigen_vec = {self.nev}", "output_path = correlators"]
         lines += [f"{k} = {v}" for k, v in self.extra.items()]
-        lines += ["[quarks]",
-                  f"quark = u:{self.n_rnd}:TB:{self.dilT}:EI:{self.dilE}:DF:4:synthetic",
-                  "[operator_lists]"]
+        quarks = self.quark_lines or (
+            f"u:{self.n_rnd}:TB:{self.dilT}:EI:{self.dilE}:DF:4:synthetic",)
+        lines += ["[quarks]"] + [f"quark = {q}" for q in quarks] + ["[operator_lists]"]
         lines += [f"operator_list = {o}" for o in self.operators]
         lines += ["[correlator_lists]"]
         lines += [f"correlator_list = {c}" for c in self.correlators]

@@ -41,14 +41,18 @@ def test_sample_extrapolation_is_a_lower_bound(engine_lib, oracle_lib):
     vdv = oracle.vdaggerv(d, gd.plan, V)
     threads = oracle.threads()
     oracle.set_threads(1)
+    # best of three of each, so that load from other processes does not decide
+    full, cold, steady = float("inf"), float("inf"), float("inf")
     try:
-        t0 = time.perf_counter()
-        oracle.contract(d, gd.plan_ptr, vdv, peram, noise, 0, 1, gd.output_doubles())
-        full = time.perf_counter() - t0
-        cold, steady = oracle.contract_sample(d, gd.plan_ptr, vdv, peram, noise, [1])
+        for _ in range(3):
+            t0 = time.perf_counter()
+            oracle.contract(d, gd.plan_ptr, vdv, peram, noise, 0, 1, gd.output_doubles())
+            full = min(full, time.perf_counter() - t0)
+            c, st = oracle.contract_sample(d, gd.plan_ptr, vdv, peram, noise, [1])
+            cold, steady = min(cold, c[0]), min(steady, st[0])
     finally:
         oracle.set_threads(threads)
     n = len(oracle.block_pair_slices(w.Lt, w.dilT, 1))
-    estimate = cold[0] + (n - 1) * steady[0]
-    assert cold[0] > steady[0] > 0
+    estimate = cold + (n - 1) * steady
+    assert cold > steady > 0
     assert 0.5 * full <= estimate <= 1.1 * full, (estimate, full)

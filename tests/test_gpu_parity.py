@@ -579,3 +579,49 @@ def test_vdaggerv_read_missing_files(tmp_path):
         eng.vdaggerv_read(str(tmp_path / "nothing"), 1)
     with pytest.raises(SlaphError, match="NOR"):
         eng.vdaggerv_read(str(tmp_path / "nothing"), 1, liuming=True)
+
+
+# ---------------------------------------------------------------- large-config features, small size
+def test_pipi_kk_displaced_smeared_two_flavours_match_oracle(oracle_lib, tmp_path):
+    """The feature set of the 48^3x96 pipi I=1 + KK workload at a size the
+    oracle runs in seconds: two quark flavours (u, s) with 5 random vectors
+    each, the pipi diagrams (C2c, C3c, C4cB/D/V) and the KK ones (C2c, C4cD,
+    C4cC, C20, C40B/C/D/V, infiles/KK.in), a one-derivative displaced operator
+    on links HYP-smeared on the device (infile alpha1, alpha2, iterations), in
+    both precisions against the oracle."""
+    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300.engine import OperatorFactory
+    ops = ["g5.d0.p0,1", "g1.d0.p0,1", "g4.d0.p0", "g5.d>x.p0"]
+    corr = ["C2c:Q0:Op0:Q0:Op0:P0,1", "C3c:Q0:Op0:Q0:Op1:Q0:Op0:P0,1",
+            "C4cB:Q0:Op0:Q0:Op0:Q0:Op0:Q0:Op0:P0,1", "C4cD:Q0:Op0:Q0:Op0:Q0:Op0:Q0:Op0:P0",
+            "C4cV:Q0:Op0:Q0:Op0:Q0:Op0:Q0:Op0:P0",
+            "C2c:Q0:Op0:Q1:Op0:P0", "C4cD:Q0:Op0:Q1:Op0:Q0:Op0:Q1:Op0:P0",
+            "C4cC:Q0:Op0:Q1:Op0:Q0:Op0:Q1:Op0:P0", "C20:Q0:Op2:Q1:Op2:P0",
+            "C40D:Q0:Op2:Q1:Op2:Q0:Op2:Q1:Op2:P0", "C40V:Q0:Op2:Q1:Op2:Q0:Op2:Q1:Op2:P0",
+            "C40C:Q0:Op2:Q1:Op2:Q0:Op2:Q1:Op2:P0", "C40B:Q0:Op2:Q1:Op2:Q0:Op2:Q1:Op2:P0",
+            "C2c:Q0:Op3:Q0:Op3:P0"]
+    w = synthetic.Workload("pipi_kk_disp", Lt=8, L=4, nev=8, n_rnd=10, dilT=2, dilE=2,
+                           operators=ops, correlators=corr,
+                           quark_lines=("u:5:TB:2:EI:2:DF:4:synthetic",
+                                        "s:5:TB:2:EI:2:DF:4:synthetic"),
+                           extra={"alpha1": 0.62, "alpha2": 0.62, "iterations": 2}, seed=55)
+    gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+    assert gd.dims.n_rnd == 10
+    assert any(gd.plan.vdv_ops[k].n_disp > 0 for k in range(gd.plan.n_vdv_ops))
+    V, peram, noise = workload_inputs(w)
+    U = _fixture_links(4, 8, seed=9)
+    a1, a2, n_hyp = gd.hyp_parameters()
+    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=oracle.smear_hyp(gd.dims, U, a1, a2, n_hyp))
+    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+                          gd.output_doubles()).reshape(-1, gd.dims.Lt)
+    assert np.max(np.abs(ref)) > 0
+    for precision in (0, 1):
+        eng = make_engine(gd, V, peram, noise)
+        fac = OperatorFactory(eng, gd)
+        fac.set_gauge_field(U)
+        fac.create_operators(precision)
+        out = eng.contract(gd.plan_ptr, precision, 0)
+        err = rel_err(out, ref)
+        print(f"pipi + KK + displaced, smeared, two flavours: precision {precision} "
+              f"max rel err {err:.2e} over {ref.shape[0]} correlators")
+        assert err < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
