@@ -625,3 +625,40 @@ def test_pipi_kk_displaced_smeared_two_flavours_match_oracle(oracle_lib, tmp_pat
         print(f"pipi + KK + displaced, smeared, two flavours: precision {precision} "
               f"max rel err {err:.2e} over {ref.shape[0]} correlators")
         assert err < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
+
+
+# ---------------------------------------------------------------- uneven workloads in one process
+UNEVEN = [(4, 8, 8, 3, 2, 2), (6, 8, 12, 4, 4, 2), (4, 12, 16, 5, 4, 4),
+          (6, 6, 8, 6, 2, 2), (4, 8, 20, 3, 8, 4), (8, 8, 12, 4, 2, 4)]
+
+
+def test_uneven_configurations_in_one_process_match_oracle(oracle_lib, tmp_path):
+    """Several configurations of different lattice size, Nev, random-vector
+    count and time dilution (L, Lt, Nev, n_rnd, dilT, dilE above) through
+    engines that are all alive at once, their VdaggerV builds and contractions
+    interleaved (each engine owns its buffers and streams); every instance
+    against the oracle, both precisions."""
+    from slaph_gb300 import GlobalData, synthetic
+    cases = []
+    for i, (L, Lt, nev, nr, dT, dE) in enumerate(UNEVEN):
+        corr = ["C2c:Q0:Op0:Q0:Op0:P0,1", "C3c:Q0:Op0:Q0:Op1:Q0:Op0:P0,1"]
+        if nr >= 4:
+            corr.append("C4cD:Q0:Op0:Q0:Op0:Q0:Op0:Q0:Op0:P0,1")
+        w = synthetic.Workload(f"uneven{i}", Lt=Lt, L=L, nev=nev, n_rnd=nr, dilT=dT, dilE=dE,
+                               operators=["g5.d0.p0,1", "g1.d0.p0,1"], correlators=corr,
+                               seed=70 + i)
+        gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+        V, peram, noise = workload_inputs(w)
+        vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
+        ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+                              gd.output_doubles()).reshape(-1, Lt)
+        cases.append((gd, make_engine(gd, V, peram, noise), ref))
+    for precision in (1, 0):
+        for gd, eng, _ in cases:
+            eng.vdaggerv_build(precision)
+        outs = [eng.contract(gd.plan_ptr, precision, 0) for gd, eng, _ in reversed(cases)]
+        for (gd, eng, ref), out in zip(cases, reversed(outs)):
+            err = rel_err(out, ref)
+            print(f"uneven {tuple(gd.dims.__getattribute__(k) for k in ('Lx', 'Lt', 'nev', 'n_rnd', 'dilT', 'dilE'))}"
+                  f" precision {precision}: max rel err {err:.2e}")
+            assert err < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
