@@ -3,6 +3,8 @@ include/slaph_gb300.h declares (no compute calls)."""
 import re
 from pathlib import Path
 
+import pytest
+
 from conftest import REPO
 
 
@@ -52,3 +54,27 @@ def test_io_names_match_the_reference_fixture_tree(l4):
                                       "randomvector.rndvecnb02.s.nbev0016.1000")
     assert gd.io_name(1000, 3) == "_cnfg1000.h5"
     assert gd.io_name(1000, 4) == "/hiskp4/gauges/quenched/wilson_b5.85_L12T24/conf.1000"
+
+
+def test_header_compiles_as_c_and_the_frontend_runs_from_c(engine_lib, tmp_path):
+    """include/slaph_gb300.h from a C99 program (gcc -pedantic, no C++), linked
+    against the library: parse the L4 infile and read names, no GPU needed."""
+    import shutil
+    import subprocess
+    from conftest import GOLDEN
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    lib = Path(engine_lib._name)
+    exe = tmp_path / "abi_frontend"
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                    "-I", str(REPO / "include"), str(REPO / "tests" / "c" / "abi_frontend.c"),
+                    "-o", str(exe), str(lib), f"-Wl,-rpath,{lib.parent}"], check=True)
+    out = subprocess.run([str(exe), str(GOLDEN / "l4" / "test_all.ini")], check=True,
+                         capture_output=True, text=True).stdout
+    assert "dims 4 4 4 4 nev 16 dilT 2 dilE 2 n_rnd 10" in out, out
+    assert "start 1000" in out
+    assert ("peram light/cnfg1000/rnd_vec_00/perambulator.rndvecnb00.u.TsoB0002.VsoI0002."
+            "DsoF4.TsiF0004.SsiF0064.DsiF4.CsiF3.smeared0.01000") in out
+    assert "vdv //cache/cnfg1000/operators.1000.p_" in out
+    assert "error unknown integer setting 'no_such_key'" in out
