@@ -662,3 +662,47 @@ def test_uneven_configurations_in_one_process_match_oracle(oracle_lib, tmp_path)
             print(f"uneven {tuple(gd.dims.__getattribute__(k) for k in ('Lx', 'Lt', 'nev', 'n_rnd', 'dilT', 'dilE'))}"
                   f" precision {precision}: max rel err {err:.2e}")
             assert err < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
+
+
+# ---------------------------------------------------------------- the ABI from C
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c_caller_writes_the_reference_goldens(l4, tmp_path, precision):
+    """tests/c/abi_contract.c, a plain C99 caller of the ABI, runs the L4
+    integration case (infile, inputs, VdaggerV, contraction, HDF5 output per
+    diagram); its files hold the reference's 2307 golden datasets (h5diff
+    -d 1e-12 in FP64, 1e-10 relative in the split-precision path)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    from conftest import GOLDEN, REPO
+    from h5lite import read_correlators
+    from slaph_gb300 import _lib
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    lib = Path(_lib.lib()._name)
+    exe = tmp_path / "abi_contract"
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                    "-I", str(REPO / "include"), str(REPO / "tests" / "c" / "abi_contract.c"),
+                    "-o", str(exe), str(lib), f"-Wl,-rpath,{lib.parent}"], check=True)
+    inp, out = tmp_path / "in", tmp_path / "out"
+    inp.mkdir()
+    out.mkdir()
+    for t, v in enumerate(l4["V"]):
+        np.ascontiguousarray(v).tofile(inp / f"V_{t}.bin")
+    for r, p in enumerate(l4["peram"]):
+        np.ascontiguousarray(p).tofile(inp / f"P_{r}.bin")
+        np.ascontiguousarray(l4["noise"][r]).tofile(inp / f"N_{r}.bin")
+    run = subprocess.run([str(exe), str(GOLDEN / "l4" / "test_all.ini"), str(inp), str(out),
+                          str(precision)], capture_output=True, text=True)
+    assert run.returncode == 0, run.stderr
+    golden = l4["golden"]
+    scale = max(float(np.max(np.abs(v))) for v in golden.values())
+    n, worst = 0, 0.0
+    for f in sorted(out.glob("*.h5")):
+        for name, val in read_correlators(f).items():
+            worst = max(worst, float(np.max(np.abs(val - golden[name]))))
+            n += 1
+    print(f"C caller, precision {precision}: {n} datasets, max |C - golden| {worst:.2e}")
+    assert n == len(golden) == 2307
+    assert worst < (1e-12 if precision == 0 else 1e-10 * scale)
