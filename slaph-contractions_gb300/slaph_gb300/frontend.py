@@ -181,6 +181,37 @@ def vdaggerv_file_name(path_vdaggerv, config, op, t=0, kind=VDV_FILE_WRITE):
     return buf.value.decode()
 
 
+def read_eigenvectors(path, dim_row, nev):
+    """One eigenvector timeslice file (slaph_read_eigenvectors): complex
+    (nev, dim_row), i.e. the column-major (dim_row x nev) block Engine takes."""
+    import numpy as np
+    out = np.zeros((nev, dim_row), np.complex128)
+    L.check(L.lib().slaph_read_eigenvectors(str(path).encode(), dim_row, nev,
+                                            out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+def read_perambulator(path, Lt, nev, dilT, dilE, dilD=4):
+    """One perambulator file (slaph_read_perambulator), re-sorted: complex
+    (cols, rows) = column-major storage of the (4 nev Lt) x (Lt/dilT dilE dilD)
+    matrix."""
+    import numpy as np
+    rows, cols = 4 * nev * Lt, (Lt // dilT) * dilE * dilD
+    out = np.zeros((cols, rows), np.complex128)
+    L.check(L.lib().slaph_read_perambulator(str(path).encode(), Lt, nev, dilT, dilE, dilD,
+                                            out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+def read_random_vector(path, length):
+    """One random vector file (slaph_read_random_vector): complex (length,)."""
+    import numpy as np
+    out = np.zeros(length, np.complex128)
+    L.check(L.lib().slaph_read_random_vector(str(path).encode(), length,
+                                             out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
 def read_gauge_lime(path, Lt, Lx, Ly, Lz, n_dir=3):
     """Gauge links of a LIME/ILDG file (slaph_read_gauge_lime): complex array
     (Lt, Lx*Ly*Lz, n_dir, 9), each link column-major, directions x, y, z (and

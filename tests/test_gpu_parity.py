@@ -706,3 +706,35 @@ def test_c_caller_writes_the_reference_goldens(l4, tmp_path, precision):
     print(f"C caller, precision {precision}: {n} datasets, max |C - golden| {worst:.2e}")
     assert n == len(golden) == 2307
     assert worst < (1e-12 if precision == 0 else 1e-10 * scale)
+
+
+# ---------------------------------------------------------------- the command line
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_command_line_reproduces_the_reference_goldens(l4, tmp_path, precision):
+    """`python -m slaph_gb300 -i test_all.ini --start_config 1000 --end_config
+    1000`, as the reference's integration test runs `contract`
+    (tests/integration-L4/run-integration-test:14), in a directory holding the
+    L4 inputs in the reference's formats and file names: its HDF5 files hold
+    the reference's 2307 golden datasets."""
+    import shutil
+    from conftest import GOLDEN
+    from h5lite import read_correlators
+    from reference_files import write_inputs
+    from test_reference_files import cli
+    shutil.copy(GOLDEN / "l4" / "test_all.ini", tmp_path / "test_all.ini")
+    write_inputs(l4["gd"], 1000, l4["V"], l4["peram"], l4["noise"], tmp_path)
+    run = cli(["-i", "test_all.ini", "--start_config", "1000", "--end_config", "1000",
+               "--precision", precision], tmp_path)
+    assert run.returncode == 0, run.stderr
+    golden = l4["golden"]
+    scale = max(float(np.max(np.abs(v))) for v in golden.values())
+    files = sorted((tmp_path / "correlators").glob("*_cnfg1000.h5"))
+    n, worst = 0, 0.0
+    for f in files:
+        for name, val in read_correlators(f).items():
+            worst = max(worst, float(np.max(np.abs(val - golden[name]))))
+            n += 1
+    print(f"command line, {precision}: {len(files)} files, {n} datasets, "
+          f"max |output - golden| {worst:.2e}")
+    assert len(files) == 18 and n == len(golden) == 2307
+    assert worst < (1e-12 if precision == "fp64" else 1e-10 * scale)
