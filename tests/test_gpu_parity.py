@@ -738,3 +738,45 @@ def test_command_line_reproduces_the_reference_goldens(l4, tmp_path, precision):
           f"max |output - golden| {worst:.2e}")
     assert len(files) == 18 and n == len(golden) == 2307
     assert worst < (1e-12 if precision == "fp64" else 1e-10 * scale)
+
+
+def test_command_line_displaced_operators_smeared_links_match_oracle(oracle_lib, tmp_path):
+    """The command line on a workload with displaced operators and HYP
+    parameters: it reads the gauge configuration from <path_config>/conf.%04d
+    (the reference's 4^4 LIME file), smears it, builds displaced VdaggerV and
+    writes correlators equal to the oracle's."""
+    import shutil
+    from conftest import GOLDEN
+    from h5lite import read_correlators
+    from reference_files import write_inputs
+    from slaph_gb300 import GlobalData, synthetic
+    from test_reference_files import cli
+    ops = ["g5.d0.p0,1", "g5.d>x.p0", "g5.d<y|>z.p0"]
+    w = synthetic.Workload("cli_disp", Lt=4, L=4, nev=8, n_rnd=4, dilT=2, dilE=2, operators=ops,
+                           correlators=[f"C2c:Q0:Op{k}:Q0:Op{k}:P0" for k in range(len(ops))]
+                           + ["C4cD:Q0:Op1:Q0:Op1:Q0:Op1:Q0:Op1:P0"],
+                           extra={"alpha1": 0.62, "alpha2": 0.62, "iterations": 2,
+                                  "path_config": "gauge"}, seed=23)
+    infile = w.write_infile(str(tmp_path))
+    gd = GlobalData.from_infile(infile)
+    assert gd.plan.need_gaugefield
+    V, peram, noise = workload_inputs(w)
+    write_inputs(gd, 1, V, peram, noise, tmp_path)
+    (tmp_path / "gauge").mkdir()
+    shutil.copy(GOLDEN / "l4" / "gauge_conf.1000", tmp_path / "gauge" / "conf.0001")
+    run = cli(["-i", infile, "--precision", "mixed"], tmp_path)
+    assert run.returncode == 0, run.stderr
+    from slaph_gb300.frontend import read_gauge_lime
+    U = [np.ascontiguousarray(u) for u in read_gauge_lime(GOLDEN / "l4" / "gauge_conf.1000",
+                                                          4, 4, 4, 4, 3)]
+    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=oracle.smear_hyp(gd.dims, U, 0.62, 0.62, 2))
+    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+                          gd.output_doubles()).reshape(-1, gd.dims.Lt)
+    expect = dict(zip([n for _, ds in gd.output_layout() for n in ds], ref))
+    got = {}
+    for f in (tmp_path / "correlators").glob("*_cnfg0001.h5"):
+        got.update(read_correlators(f))
+    assert set(got) == set(expect)
+    err = max(float(np.max(np.abs(got[k] - expect[k]))) for k in expect) / np.max(np.abs(ref))
+    print(f"command line, displaced + smeared: {len(got)} datasets, max rel err {err:.2e}")
+    assert err < REL_MIXED_CORR
