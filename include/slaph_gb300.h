@@ -282,6 +282,13 @@ int slaph_engine_smear_gauge_hyp(slaph_engine *eng, double alpha1, double alpha2
  * the slaph_engine_set_gauge layout. */
 int slaph_engine_gauge_fetch(slaph_engine *eng, int32_t t, double *out);
 
+/* Self-test of the bounded device waits that every tensor-core pipeline stage
+ * uses: one kernel waits on an mbarrier that nothing completes, gives up after
+ * `cycles` clock cycles and reports it (*device_code = 1); the context stays
+ * usable.  Returns SLAPH_OK when the wait gave up as designed.  No
+ * counterpart in the reference (it has no device code). */
+int slaph_selftest_bounded_wait(int64_t cycles, int32_t *device_code);
+
 /* Page-locked host memory for the inputs, so that the set_* copies above run
  * at the full host-device link rate.  slaph_host_alloc returns driver-pinned
  * memory (cudaHostAlloc) that keeps that rate for its whole lifetime; free it

@@ -76,6 +76,24 @@ int slaph_engine_gauge_fetch(slaph_engine *eng, int32_t t, double *out) {
   return slaph::guarded([&] { get(eng).gauge_fetch(t, out); });
 }
 
+int slaph_selftest_bounded_wait(int64_t cycles, int32_t *device_code) {
+  return slaph::guarded([&] {
+    if (!device_code || cycles < 0) throw slaph::ArgError("invalid argument");
+    int *err = nullptr;
+    slaph::cuda_check(cudaMalloc(&err, sizeof(int)), "cudaMalloc");
+    int code = 0;
+    cudaError_t e = cudaMemset(err, 0, sizeof(int));
+    if (e == cudaSuccess) e = slaph::dev::bounded_wait_selftest(err, cycles, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&code, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(err);
+    slaph::cuda_check(e, "bounded wait self-test");
+    *device_code = code;
+    if (code != 1)
+      throw slaph::CudaError("bounded wait self-test: the device wait did not give up as designed");
+  });
+}
+
 int slaph_host_alloc(size_t bytes, void **out) {
   return slaph::guarded([&] {
     if (!out || bytes == 0) throw slaph::ArgError("null output or empty size");

@@ -118,6 +118,9 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
                         VdvDisplaced const *disp = nullptr);
 // (t_ready[t], when given and non-null: event after which timeslice t of V is
 // valid; the slicing of t waits for it on `stream`.)
+// One bounded mbarrier wait that nothing completes (selftest.cu): *err = 1
+// once it gives up after `cycles` clock cycles.
+cudaError_t bounded_wait_selftest(int *err, long long cycles, cudaStream_t stream);
 // Identity blocks for code 2*op (and 2*op+1).
 cudaError_t vdaggerv_identity(double2 *vdv, int32_t op, Geometry g, cudaStream_t stream);
 // vdv[2*op+1][t] = vdv[2*op][t]^H for all ops, t.

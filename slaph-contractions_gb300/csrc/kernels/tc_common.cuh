@@ -92,16 +92,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false (and *err = code) when the phase did not complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+// Bounded wait: false (and *err = code) when the phase did not complete
+// within `limit` clock cycles.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, uint32_t parity, int *err, int code,
+                                              long long limit) {
   long long const t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) {
+    if (clock64() - t0 > limit) {
       atomicCAS(err, 0, code);
       return false;
     }
   }
   return true;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+  return mbar_wait_for(bar, parity, err, code, kWaitCycles);
 }
 __device__ __forceinline__ void bulk_g2s(void *dst, void const *src, uint32_t bytes,
                                          uint64_t *bar) {

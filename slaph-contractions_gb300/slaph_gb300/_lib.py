@@ -123,6 +123,7 @@ PROTOTYPES = {
     "slaph_engine_set_gauge": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_engine_smear_gauge_hyp": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _i32]),
     "slaph_engine_gauge_fetch": (C.c_int, [C.c_void_p, _i32, _dp]),
+    "slaph_selftest_bounded_wait": (C.c_int, [_i64, C.POINTER(_i32)]),
     "slaph_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "slaph_host_free": (C.c_int, [C.c_void_p]),
     "slaph_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),

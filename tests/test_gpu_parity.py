@@ -780,3 +780,22 @@ def test_command_line_displaced_operators_smeared_links_match_oracle(oracle_lib,
     err = max(float(np.max(np.abs(got[k] - expect[k]))) for k in expect) / np.max(np.abs(ref))
     print(f"command line, displaced + smeared: {len(got)} datasets, max rel err {err:.2e}")
     assert err < REL_MIXED_CORR
+
+
+# ---------------------------------------------------------------- bounded device waits
+def test_bounded_device_wait_gives_up_and_the_context_stays_usable(l4):
+    """The bounded mbarrier wait of the tensor-core pipelines
+    (slaph_selftest_bounded_wait): a wait that nothing completes gives up after
+    its limit, the kernel reports it and exits, and the same context then runs
+    a VdaggerV build and a contraction correctly."""
+    import ctypes as C
+    from slaph_gb300 import _lib as L
+    code = C.c_int32(0)
+    L.check(L.lib().slaph_selftest_bounded_wait(200000, C.byref(code)))
+    assert code.value == 1
+    eng = make_engine(l4["gd"], l4["V"], l4["peram"], l4["noise"])
+    eng.vdaggerv_build(1)
+    out = eng.contract(l4["gd"].plan_ptr, 1, 0)
+    golden = l4["golden"]
+    names = [n for _, ds in l4["gd"].output_layout() for n in ds]
+    assert max(float(np.max(np.abs(v - golden[n]))) for n, v in zip(names, out)) < 1e-10
