@@ -39,21 +39,26 @@ for p in (str(REPO), str(REPO / "slaph-contractions_gb300")):
 METRIC = "s/gauge-config, VdaggerV+pipi contractions 32³×64: FP64 vs split-prec @1e-10"
 UNIT = "s/gauge-config"
 
-# DRAM bytes (read + write) per trace entry of the double-float trace kernel,
-# from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum of one
-# launch divided by its trace entries) on the 16^3x32 Nev=64 pipi case, keyed
-# by dilE; the kernel's traffic scales with its trace entries.
-NCU_TRACE_DRAM_BYTES_PER_ENTRY = {8: 2280.0}
-# The same for the tensor-core trace GEMM (DRAM bytes per dense-group entry):
-# the 58 trace-group launches of one 32^3x64 configuration moved 1368.2 GB for
-# 5.09e9 entries (one capture of dram__bytes_read/write.sum over the full-size
-# bench command), keyed by dilE.
-NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY = {8: 268.8}
-# DRAM bytes of the split-precision VdaggerV stage (colmax, slice_a, slice_b,
-# ozaki_gemm kernels) per computed (operator, timeslice), from the same
-# capture: 1974.3 GB for 16 operators x 64 timeslices at 32^3, Nev 220.  Keyed
-# by workload, since it depends on the lattice and Nev.
-NCU_VDV_STAGE_DRAM_BYTES_PER_UNIT = {"cfg3_32x64_pipi": 1.928e9}
+# DRAM bytes (read + write) of the tensor-core kernels per unit of work, from
+# ncu captures of dram__bytes_read.sum + dram__bytes_write.sum on the small
+# 16^3x32 Nev=64 pipi case (one kernel, a few launches, a few GB on the device),
+# scaled to a full launch by the units it processes; the capture and its
+# scaling are in the profile summaries named here.  Empty: no capture yet, the
+# roofline's traffic is then null.
+NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY = {}  # keyed by dilE, per dense-group entry
+NCU_TRACE_GEMM_TRAFFIC_SOURCE = "profiles/trace_gemm_kernel_prof_16x32_pipi.md"
+NCU_VDV_GEMM_DRAM_BYTES_PER_UNIT = {}  # keyed by workload, per (operator, timeslice)
+NCU_VDV_GEMM_TRAFFIC_SOURCE = "profiles/ozaki_gemm_kernel_prof_16x32_pipi.md"
+
+
+def per_correlator_rel_err(out, ref):
+    """Largest relative error over correlators, each (one HDF5 dataset, Lt
+    values) normalised by its own largest |value|; correlators that are zero in
+    ref contribute their absolute error."""
+    scale = np.max(np.abs(ref), axis=1)
+    diff = np.max(np.abs(out - ref), axis=1)
+    rel = np.where(scale > 0, diff / np.where(scale > 0, scale, 1.0), diff)
+    return float(np.max(rel)) if rel.size else 0.0
 
 
 def load_peaks():
@@ -287,14 +292,38 @@ def run_engine(args):
     h2d = sum(v.nbytes for v in V) + sum(p.nbytes for p in peram) + noise.nbytes
     d2h = out.nbytes
 
+    # ---- the plain FP64 path on the same inputs (outside the timed regions):
+    # its time per configuration and every correlator of the split-precision
+    # result against it, relative per correlator.
+    fp64 = None
+    if precision == 1 and not args.no_fp64_check:
+        w0 = time.time()
+        eng.vdaggerv_build(0)
+        t_v = eng.timings()
+        out64 = eng.contract(gd.plan_ptr, 0, 0, args.single_block_pair)
+        t_c = eng.timings()
+        wall64 = time.time() - w0
+        st64 = [t_v[0], t_c[1], t_c[2], t_c[3]]
+        fp64 = {"value": float(sum(st64)) / 1e3, "unit": UNIT,
+                "stages_ms": dict(zip(["vdaggerv", "factors", "products_traces", "assembly"],
+                                      map(float, st64))),
+                "wall_s": wall64,
+                "max_rel_err_vs_fp64": per_correlator_rel_err(out, out64),
+                "n_correlators": int(out64.shape[0]),
+                "error_measure": ("max over correlators of max_t |mixed - fp64| / "
+                                  "max_t |fp64| (each HDF5 dataset by its own scale)")}
+
     stats = eng.stats()
     n_ops = gd.plan.n_vdv_ops - (1 if gd.plan.index_of_unity >= 0 else 0)
     vdv_flops = w.flops_vdaggerv(n_ops)
     stage_ms = stage / args.steps
     peaks = load_peaks() or {}
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    # The tensor-core kernels run inside a seconds-long step: the sustained
+    # bf16 rate is their denominator.
+    bf16_peak = peaks.get("bf16_tflops_sustained", 1700.0)
     note = "of measured" if peaks else "of fallback"
+    peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks
+                else "fallback 1.7 PFLOP/s sustained")
     names = ["vdaggerv", "factors", "products_traces", "assembly"]
     eds = 4 * w.dilE
     K = args.steps
@@ -302,10 +331,11 @@ def run_engine(args):
     kernels_ms = {"trace_gemm_kernel": ktim[8] / K, "trace_slice_kernels": ktim[10] / K,
                   "trace_df_kernel (residual lists)" if precision == 1 else "trace_kernel":
                   ktim[6] / K,
-                  "vdaggerv stage (ozaki_gemm_kernel + slicing)" if precision == 1
+                  "ozaki_gemm_kernel (VdaggerV GEMM)": ktim[11] / K,
+                  "vdaggerv stage (slicing + ozaki_gemm_kernel)" if precision == 1
                   else "vdaggerv stage (vdv_fp64_kernel)": stage_ms[0],
-                  "factor stage (q*_kernels)": stage_ms[1]}
-    # Roofline candidates: (time per step in ms, launches per step, roofline).
+                  "factor stage (q*_kernels, factor GEMMs)": stage_ms[1]}
+    # Roofline candidates, one kernel each: (time per step in ms, roofline).
     cands = []
     if precision == 1 and ktim[8] > 0:
         # Dense trace groups: per entry 8 (4dilE)^2 FP64-equivalent flops,
@@ -314,37 +344,29 @@ def run_engine(args):
         n_l = ktim[9] / K
         cands.append((ktim[8] / K, {
             "kernel": "trace_gemm_kernel", "bound": "tensor",
-            "achieved": flops / n_l / (ktim[8] / K / n_l / 1e3) / 1e12, "peak": bf16_peak,
-            "unit": "TFLOP/s", "peak_source": f"MEASURED_PEAKS.json bf16_tflops ({note})",
+            "achieved": flops / (ktim[8] / K / 1e3) / 1e12, "peak": bf16_peak,
+            "unit": "TFLOP/s", "peak_source": f"{peak_src} ({note})",
             "launches_per_step": n_l, "launch_ms_avg": ktim[8] / K / n_l,
             "algorithmic_per_launch": flops / n_l,
             "traffic": (NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY.get(w.dilE, 0) * stats[7] / n_l)
             or None,
+            "traffic_source": NCU_TRACE_GEMM_TRAFFIC_SOURCE,
             "fp64_equivalent_tflops": 8.0 * eds * eds * stats[7] / (ktim[8] / K / 1e3) / 1e12,
             "work": "21 split-BF16 products x 8 (4dilE)^2 flops per dense-group trace entry"}))
-    if precision == 1 and stage_ms[0] > 0:
+    if precision == 1 and ktim[11] > 0:
         flops = 21 * vdv_flops  # 21 slice pairs of the real form of every (op, t) product
-        cands.append((stage_ms[0], {
-            "kernel": "ozaki_gemm_kernel (+ slicing)", "bound": "tensor",
-            "achieved": flops / (stage_ms[0] / 1e3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
-            "peak_source": f"MEASURED_PEAKS.json bf16_tflops ({note})",
-            "traffic": (NCU_VDV_STAGE_DRAM_BYTES_PER_UNIT.get(args.workload, 0)
-                        * n_ops * w.Lt) or None,
-            "traffic_unit": "bytes per configuration (the stage's kernels together)",
-            "fp64_equivalent_tflops": vdv_flops / (stage_ms[0] / 1e3) / 1e12,
+        n_l = ktim[12] / K
+        cands.append((ktim[11] / K, {
+            "kernel": "ozaki_gemm_kernel", "bound": "tensor",
+            "achieved": flops / (ktim[11] / K / 1e3) / 1e12, "peak": bf16_peak,
+            "unit": "TFLOP/s", "peak_source": f"{peak_src} ({note})",
+            "launches_per_step": n_l, "launch_ms_avg": ktim[11] / K / n_l,
+            "algorithmic_per_launch": flops / n_l,
+            "traffic": (NCU_VDV_GEMM_DRAM_BYTES_PER_UNIT.get(args.workload, 0)
+                        * n_ops * w.Lt / n_l) or None,
+            "traffic_source": NCU_VDV_GEMM_TRAFFIC_SOURCE,
+            "fp64_equivalent_tflops": vdv_flops / (ktim[11] / K / 1e3) / 1e12,
             "work": "21 split-BF16 products x 8 nev^2 3L^3 flops per (operator, timeslice)"}))
-    if ktim[6] > 0:
-        n_l = ktim[7] / K
-        ent = stats[6] - stats[7] if precision == 1 else stats[6]
-        byt = ent * 2 * 16 * eds * eds  # both (4dilE)^2 complex operands per entry
-        cands.append((ktim[6] / K, {
-            "kernel": "trace_df_kernel" if precision == 1 else "trace_kernel", "bound": "hbm",
-            "achieved": byt / (ktim[6] / K / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-            "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({note})",
-            "traffic": (NCU_TRACE_DRAM_BYTES_PER_ENTRY.get(w.dilE, 0) * ent / n_l) or None,
-            "launches_per_step": n_l, "launch_ms_avg": ktim[6] / K / n_l,
-            "algorithmic_per_launch": byt / n_l,
-            "work": "2 x 16 (4dilE)^2 bytes of operands per trace entry (L2-reused)"}))
     ms_dom, roofline = max(cands, key=lambda c: c[0]) if cands else (0.0, {})
     if roofline:
         roofline["frac"] = roofline["achieved"] / roofline["peak"]
@@ -352,6 +374,17 @@ def run_engine(args):
     others = [c[1] for c in cands if c[1] is not roofline]
     for o in others:
         o["frac"] = o["achieved"] / o["peak"]
+    if ktim[6] > 0:
+        # The per-entry trace kernel is bound by FP32 instruction issue (its
+        # operands are reused from L2), so it gets no HBM roofline.
+        ent = stats[6] - stats[7] if precision == 1 else stats[6]
+        others.append({
+            "kernel": "trace_df_kernel" if precision == 1 else "trace_kernel",
+            "bound": "fp32-issue" if precision == 1 else "fp64-issue",
+            "ms_per_step": ktim[6] / K, "trace_entries_per_step": ent,
+            "fp64_equivalent_tflops": 8.0 * eds * eds * ent / (ktim[6] / K / 1e3) / 1e12,
+            "note": ("double-float arithmetic, about 40 FP32 instructions per complex "
+                     "multiply-add; operands reused about 14x from L2")})
     line = {
         "metric": METRIC, "value": dev_s * world / world, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3,
@@ -384,6 +417,10 @@ def run_engine(args):
         "clocks": clocks,
         "wall_s_per_step": wall / args.steps,
     }
+    if fp64 is not None:
+        line["fp64"] = fp64
+        line["fp64_value"] = fp64["value"]
+        line["max_rel_err_vs_fp64"] = fp64["max_rel_err_vs_fp64"]
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(w, gd, args)
     if rank == 0:
@@ -512,6 +549,8 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--single-block-pair", type=int, default=-1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true",
+                    help="skip the FP64 run and the per-correlator comparison after timing")
     ap.add_argument("--host-buffers", choices=["pinned", "pageable"], default="pinned",
                     help="host input buffers: driver-pinned, or pageable without huge pages")
     args = ap.parse_args()

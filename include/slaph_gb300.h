@@ -368,8 +368,10 @@ int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
  * out[4] host planning (wall clock), out[5] kernel launches issued,
  * out[6] the per-entry trace kernel alone (summed over its launches), out[7]
  * its launch count, out[8] the tensor-core trace GEMM (mixed precision),
- * out[9] its launch count, out[10] the slicing of its operands.  Returns the
- * number of values written (<= n, at most 12). */
+ * out[9] its launch count, out[10] the slicing of its operands, out[11] the
+ * split-precision VdaggerV GEMM alone (summed over its launches; set by the
+ * build), out[12] its launch count.  Returns the number of values written
+ * (<= n, at most 13). */
 int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
 
 /* VdaggerV of one operator on one timeslice for callers that cannot let a
@@ -380,11 +382,13 @@ int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
  * slaph_vdaggerv_build(SLAPH_FP64).
  *   V_t:  DEVICE pointer, 3*L^3 x nev complex, column-major (one timeslice)
  *   out:  DEVICE pointer, nev x nev complex, column-major
- *   momentum: host array of 3 ints; stream: a cudaStream_t (NULL = legacy)
+ *   momentum: host array of 3 ints, read during the call and handed to the
+ *             device as kernel arguments (the GPU reads no host memory);
+ *   stream:   a cudaStream_t (NULL = legacy)
  * Allocates nothing: the phase table lives in a static device array of
  * 4 MiB + 256 B, which every GPU that loads the library holds until the
- * process exits, so L^3 may not exceed 262144 (64^3); larger lattices are
- * rejected with SLAPH_ERR_ARG.  The first call on a device looks up that
+ * process exits, so L^3 may not exceed 262144 (64^3); larger lattices (and
+ * any single extent above that) are rejected with SLAPH_ERR_ARG.  The first call on a device looks up that
  * array's device address (once per device); make that first call before any
  * stream capture.  The work is enqueued on `stream` and not waited for.
  * Every call shares the one array: calls whose work overlaps on the GPU (other

@@ -1041,14 +1041,20 @@ int vdaggerv_impl(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
     else
       for (int t = 0; t < dims->Lt; ++t) tlist.push_back(t);
     size_t const blk = static_cast<size_t>(nev) * nev;
+    // The reference distributes timeslices over its threads
+    // (src/OperatorFactory.cpp:263-272); the (timeslice, operator) pairs are
+    // distributed here, which gives the same blocks and also keeps every
+    // thread busy when only a few timeslices are asked for.
+    size_t const n_items = tlist.size() * static_cast<size_t>(n_ops);
 #pragma omp parallel num_threads(oracle_threads())
     {
       std::vector<cd> W(static_cast<size_t>(dim_row) * nev);
 #pragma omp for schedule(dynamic)
-      for (size_t it = 0; it < tlist.size(); ++it) {
-        int const t = tlist[it];
+      for (size_t it = 0; it < n_items; ++it) {
+        int const t = tlist[it / n_ops];
+        int const o = static_cast<int>(it % n_ops);
         cd const *Vt = reinterpret_cast<cd const *>(V[t]);
-        for (int o = 0; o < n_ops; ++o) {
+        {
           cd *dst = reinterpret_cast<cd *>(out) + (static_cast<size_t>(o) * dims->Lt + t) * blk;
           if (ops[o].id == index_of_unity) {
             for (size_t i = 0; i < blk; ++i) dst[i] = 0;  // identity, :317

@@ -157,7 +157,7 @@ int slaph_engine_timings(const slaph_engine *eng, double *out, int n) {
     slaph::set_last_error("invalid argument");
     return -1;
   }
-  int const m = n < 12 ? n : 12;
+  int const m = n < 13 ? n : 13;
   for (int i = 0; i < m; ++i) out[i] = eng->e->timings[i];
   return m;
 }

@@ -126,8 +126,9 @@ Engine::~Engine() {
   if (ev_v_used_) cudaEventDestroy(ev_v_used_);
   if (ev_pn_used_) cudaEventDestroy(ev_pn_used_);
   if (up_stream_) cudaStreamDestroy(up_stream_);
-  for (auto &e : tc_ev_)
-    if (e) cudaEventDestroy(e);
+  for (auto *v : {&tc_ev_, &vdv_ev_})
+    for (auto &e : *v)
+      if (e) cudaEventDestroy(e);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -301,11 +302,24 @@ void Engine::vdaggerv_build(int precision) {
                            U_.as<double2>(), W_.as<double2>(), phase_unit_.as<longlong2>(),
                            unit_op_.as<int32_t>()};
   }
+  int32_t n_gemm = 0;
   if (precision == SLAPH_MIXED) {
     int sms = 0;
     SLAPH_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
     int32_t const batch = dev::vdaggerv_tc_batch(geo_, std::max(n_all, 1), sms, kTcScratchCap);
     tc_scratch_.reserve(dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), batch));
+    // The scratch may be larger than this batch needs (kept from an earlier
+    // call): the launch count follows from what it holds.
+    int64_t const fits = static_cast<int64_t>(
+        tc_scratch_.size() / dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), 1));
+    n_gemm = n_all > 0 ? dev::vdaggerv_tc_gemm_launches(
+                             dims_.Lt, static_cast<int32_t>(std::max<int64_t>(1, fits)))
+                       : 0;
+    while (vdv_ev_.size() < 2 * static_cast<size_t>(n_gemm)) {
+      cudaEvent_t e = nullptr;
+      SLAPH_CK(cudaEventCreate(&e));
+      vdv_ev_.push_back(e);
+    }
     err_.reserve(sizeof(int));
     SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
   }
@@ -320,7 +334,8 @@ void Engine::vdaggerv_build(int precision) {
     launch(dev::vdaggerv_tc(vdv_.as<double2>(), V_.as<double2>(), phase_fx_.as<longlong2>(),
                             list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_,
                             tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_,
-                            ready.data(), tc_disp ? &dd : nullptr),
+                            ready.data(), tc_disp ? &dd : nullptr, vdv_ev_.data(),
+                            2 * n_gemm),
            "vdaggerv_tc");
     // per timeslice three slicing kernels, and per displaced operator its
     // steps, exponents and slicing; one GEMM per timeslice batch
@@ -378,6 +393,10 @@ void Engine::vdaggerv_build(int precision) {
   SLAPH_CK(cudaEventSynchronize(ev_[1]));
   timings[0] = elapsed_ms(ev_[0], ev_[1]);
   timings[5] = static_cast<double>(launches_);
+  double t_gemm = 0;
+  for (int32_t k = 0; k < n_gemm; ++k) t_gemm += elapsed_ms(vdv_ev_[2 * k], vdv_ev_[2 * k + 1]);
+  timings[11] = t_gemm;
+  timings[12] = static_cast<double>(n_gemm);
   if (precision == SLAPH_MIXED) {
     int code = 0;
     SLAPH_CK(cudaMemcpy(&code, err_.as<void>(), sizeof(int), cudaMemcpyDeviceToHost));

@@ -101,7 +101,7 @@ class Engine {
   void contract(slaph_plan const *plan, int precision, int accumulator, int single_block_pair,
                 double *corr_out);
 
-  double timings[12] = {};
+  double timings[16] = {};
   double stats[8] = {};
 
  private:
@@ -117,6 +117,7 @@ class Engine {
   std::vector<char> pend_v_, pend_p_, pend_n_;
   cudaEvent_t ev_v_used_ = nullptr, ev_pn_used_ = nullptr;
   std::vector<cudaEvent_t> tc_ev_;  // three per tensor-core trace batch
+  std::vector<cudaEvent_t> vdv_ev_;  // two per split-precision VdaggerV GEMM launch
 
   DevBuf V_, peram_, noise_, phase_, phase_fx_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
   std::vector<slaph_vdv_op> ops_;

@@ -115,9 +115,13 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
                         int32_t const *ops, int32_t n_comp, int32_t t0, int32_t nt, Geometry g,
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
                         cudaEvent_t const *t_ready = nullptr,
-                        VdvDisplaced const *disp = nullptr);
+                        VdvDisplaced const *disp = nullptr,
+                        cudaEvent_t const *gemm_ev = nullptr, int32_t n_gemm_ev = 0);
 // (t_ready[t], when given and non-null: event after which timeslice t of V is
-// valid; the slicing of t waits for it on `stream`.)
+// valid; the slicing of t waits for it on `stream`.  gemm_ev: when given, the
+// events 2k and 2k+1 are recorded on `stream` just before and after the k-th
+// GEMM launch, for k < n_gemm_ev / 2; vdaggerv_tc_gemm_launches gives k's range.)
+int32_t vdaggerv_tc_gemm_launches(int32_t nt, int32_t batch);
 // One bounded mbarrier wait that nothing completes (selftest.cu): *err = 1
 // once it gives up after `cycles` clock cycles.
 cudaError_t bounded_wait_selftest(int *err, long long cycles, cudaStream_t stream);

@@ -52,6 +52,18 @@ void *scratch_for_current_device() {
   return g_scratch_ptr[dev];
 }
 
+// Writes the launch metadata into the scratch from kernel arguments, so that
+// no host memory is read by the GPU: meta[0] = operator index 0 (the output
+// block), meta[1..3] = momentum.
+__global__ void noalloc_meta_kernel(int32_t *meta, int32_t px, int32_t py, int32_t pz) {
+  if (threadIdx.x == 0) {
+    meta[0] = 0;
+    meta[1] = px;
+    meta[2] = py;
+    meta[3] = pz;
+  }
+}
+
 }  // namespace
 
 extern "C" int slaph_vdaggerv_noalloc(const slaph_dims *dims, const double *V_t,
@@ -60,6 +72,12 @@ extern "C" int slaph_vdaggerv_noalloc(const slaph_dims *dims, const double *V_t,
     if (!dims || !V_t || !momentum || !out) throw slaph::ArgError("null argument");
     if (dims->Lx < 1 || dims->Ly < 1 || dims->Lz < 1 || dims->nev < 1)
       throw slaph::ArgError("invalid lattice or eigenvector count");
+    // Each extent is bounded before the product is formed, so the product
+    // (at most 2^54) cannot wrap.
+    if (static_cast<size_t>(dims->Lx) > kMaxVolume || static_cast<size_t>(dims->Ly) > kMaxVolume ||
+        static_cast<size_t>(dims->Lz) > kMaxVolume)
+      throw slaph::ArgError("slaph_vdaggerv_noalloc: a lattice extent exceeds the static "
+                            "scratch limit of " + std::to_string(kMaxVolume) + " sites (64^3)");
     size_t const vol = static_cast<size_t>(dims->Lx) * dims->Ly * dims->Lz;
     if (vol > kMaxVolume)
       throw slaph::ArgError("slaph_vdaggerv_noalloc: L^3 = " + std::to_string(vol) +
@@ -70,11 +88,8 @@ extern "C" int slaph_vdaggerv_noalloc(const slaph_dims *dims, const double *V_t,
     auto *phase = reinterpret_cast<double2 *>(base + kMetaBytes);
     cudaStream_t const s = static_cast<cudaStream_t>(stream);
 
-    // meta[0] = operator index 0 (the output block), meta[1..3] = momentum.
-    int32_t const host_meta[4] = {0, momentum[0], momentum[1], momentum[2]};
-    check(
-        cudaMemcpyAsync(meta, host_meta, sizeof host_meta, cudaMemcpyHostToDevice, s),
-        "cudaMemcpyAsync");
+    noalloc_meta_kernel<<<1, 32, 0, s>>>(meta, momentum[0], momentum[1], momentum[2]);
+    check(cudaGetLastError(), "metadata kernel");
     slaph::dev::Geometry g{};
     g.Lt = 1;
     g.Lx = dims->Lx;

@@ -226,7 +226,8 @@ cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
 cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_fx,
                         int32_t const *ops, int32_t n_comp, int32_t t0, int32_t nt, Geometry g,
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
-                        cudaEvent_t const *t_ready, VdvDisplaced const *disp) {
+                        cudaEvent_t const *t_ready, VdvDisplaced const *disp,
+                        cudaEvent_t const *gemm_ev, int32_t n_gemm_ev) {
   int32_t const n_disp = disp ? disp->n : 0;
   int32_t const n = n_comp + n_disp;
   if (n == 0 || nt == 0) return cudaSuccess;
@@ -252,6 +253,7 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
   unsigned const bb = static_cast<unsigned>((L.k_tiles * L.n_tiles * (kTN / 8) * 32 + 255) / 256);
   size_t const b_op = static_cast<size_t>(L.n_tiles * L.k_tiles) * kStageB;
   size_t const links = static_cast<size_t>(g.dim_row / 3) * 27;  // of one timeslice
+  int32_t gemm_k = 0;
   for (int32_t tb = t0; tb < t0 + nt; tb += static_cast<int32_t>(batch)) {
     int32_t const nb = static_cast<int32_t>(std::min<int64_t>(batch, t0 + nt - tb));
     for (int32_t b = 0; b < nb; ++b) {
@@ -290,6 +292,11 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
                                                 static_cast<int32_t>(L.n_tiles), g);
       }
     }
+    bool const timed = gemm_ev && 2 * gemm_k + 1 < n_gemm_ev;
+    if (timed) {
+      e = cudaEventRecord(gemm_ev[2 * gemm_k], stream);
+      if (e != cudaSuccess) return e;
+    }
     ozaki_gemm_kernel<<<dim3(static_cast<unsigned>(L.m_tiles),
                              static_cast<unsigned>(L.n_tiles),
                              static_cast<unsigned>(n * nb)),
@@ -298,8 +305,17 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
         static_cast<int32_t>(L.k_tiles), static_cast<int32_t>(L.n_tiles), tb, g, err);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (timed) {
+      e = cudaEventRecord(gemm_ev[2 * gemm_k + 1], stream);
+      if (e != cudaSuccess) return e;
+    }
+    ++gemm_k;
   }
   return cudaSuccess;
+}
+
+int32_t vdaggerv_tc_gemm_launches(int32_t nt, int32_t batch) {
+  return batch > 0 ? (nt + batch - 1) / batch : 0;
 }
 
 }  // namespace dev

@@ -156,9 +156,9 @@ class Engine:
     def timings(self):
         """ms: VdaggerV, factors, products+traces, assembly, planning; launches;
         per-entry trace kernel (ms, launches); trace GEMM (ms, launches);
-        operand slicing of the trace GEMM (ms)."""
-        out = np.zeros(12)
-        L.lib().slaph_engine_timings(self._h, L.dptr(out), 12)
+        operand slicing of the trace GEMM (ms); VdaggerV GEMM (ms, launches)."""
+        out = np.zeros(13)
+        L.lib().slaph_engine_timings(self._h, L.dptr(out), 13)
         return out
 
     def stats(self):

@@ -76,6 +76,22 @@ def l4(engine_lib):
     }
 
 
+def corr_rel_err(out, ref):
+    """Largest relative error over correlators.  Each correlator (one row of
+    Lt values, one HDF5 dataset of Diagram::write, src/Diagram.cpp:132-147) is
+    normalised by its own largest |value| over t, so a small correlator is held
+    to the same relative bound as a large one.  A correlator that is zero in
+    the reference contributes its largest |value| (an absolute error)."""
+    ref = np.asarray(ref)
+    out = np.asarray(out).reshape(ref.shape)
+    if ref.size == 0:
+        return 0.0
+    scale = np.max(np.abs(ref), axis=-1)
+    diff = np.max(np.abs(out - ref), axis=-1)
+    rel = np.where(scale > 0, diff / np.where(scale > 0, scale, 1.0), diff)
+    return float(np.max(rel))
+
+
 def workload_inputs(w):
     """Generated inputs of a synthetic workload as the oracle and engine take them."""
     V = [w.eigenvectors(t) for t in range(w.Lt)]

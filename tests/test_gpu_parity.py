@@ -3,12 +3,15 @@ reference's goldens.
 
 Tolerances: FP64 path, relative 1e-12 against the oracle and absolute 1e-12
 against the L4 goldens (the reference's own h5diff -d 1e-12 criterion).
+Correlator errors are relative per correlator (corr_rel_err: each dataset
+normalised by its own largest |value|); VdaggerV block errors are relative to
+the block's largest entry.
 """
 import numpy as np
 import pytest
 
 import oracle
-from conftest import workload_inputs
+from conftest import corr_rel_err, workload_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -17,6 +20,7 @@ ABS_GOLDEN = 1e-12
 
 
 def rel_err(a, b):
+    """Error of a matrix block relative to the block's largest entry."""
     scale = max(np.max(np.abs(b)), 1e-300)
     return np.max(np.abs(a - b)) / scale
 
@@ -58,6 +62,7 @@ def test_contract_fp64_reproduces_l4_goldens(l4, l4_engine, accumulator):
     assert out.shape == (len(names), gd.dims.Lt)
     err = max(np.max(np.abs(v - l4["golden"][n])) for n, v in zip(names, out))
     assert err < ABS_GOLDEN, err
+    assert corr_rel_err(out, np.stack([l4["golden"][n] for n in names])) < REL_FP64
 
 
 def test_contract_fp64_matches_oracle_l4(l4, l4_engine, oracle_lib):
@@ -67,6 +72,7 @@ def test_contract_fp64_matches_oracle_l4(l4, l4_engine, oracle_lib):
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     out = l4_engine.contract(gd.plan_ptr, 0, 0)
     assert np.max(np.abs(out - ref)) < 1e-13
+    assert corr_rel_err(out, ref) < REL_FP64
 
 
 def test_single_block_pair_l4(l4, l4_engine, oracle_lib):
@@ -101,7 +107,7 @@ def test_contract_fp64_matches_oracle_synthetic(name, oracle_lib):
         ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, acc, -1,
                               gd.output_doubles()).reshape(-1, gd.dims.Lt)
         out = eng.contract(gd.plan_ptr, 0, acc)
-        assert rel_err(out, ref) < REL_FP64
+        assert corr_rel_err(out, ref) < REL_FP64
 
 
 def test_two_random_vectors_raise_the_reference_error(oracle_lib):
@@ -184,8 +190,8 @@ def test_vdaggerv_mixed_matches_fp64_and_contract(name, oracle_lib):
     ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     out = eng.contract(gd.plan_ptr, 1, 0)
-    e = rel_err(out, ref)
-    print(f"{name}: mixed correlators max rel err {e:.2e}")
+    e = corr_rel_err(out, ref)
+    print(f"{name}: mixed correlators max per-correlator rel err {e:.2e}")
     assert e < REL_MIXED_CORR
 
 
@@ -204,14 +210,14 @@ def test_dense_trace_groups_match_oracle(name, oracle_lib):
             for acc in (0, 1)}
     eng.vdaggerv_build(0)
     for acc in (0, 1):
-        assert rel_err(eng.contract(gd.plan_ptr, 0, acc), refs[acc]) < REL_FP64
+        assert corr_rel_err(eng.contract(gd.plan_ptr, 0, acc), refs[acc]) < REL_FP64
     eng.vdaggerv_build(1)
     for acc in (0, 1):
         out = eng.contract(gd.plan_ptr, 1, acc)
         st, tim = eng.stats(), eng.timings()
         assert 0 < st[7] < st[6], "both dense groups and residual lists must be present"
         assert tim[9] > 0 and tim[7] > 0, "tensor-core and per-entry trace kernels must run"
-        e = rel_err(out, refs[acc])
+        e = corr_rel_err(out, refs[acc])
         print(f"{name}: mixed correlators (acc {acc}) max rel err {e:.2e}, "
               f"{st[7] / st[6]:.0%} of trace entries in dense groups")
         assert e < REL_MIXED_CORR
@@ -270,8 +276,11 @@ def test_mixed_l4_goldens(l4):
     names = [n for _, ds in gd.output_layout() for n in ds]
     scale = max(np.max(np.abs(v)) for v in l4["golden"].values())
     err = max(np.max(np.abs(v - l4["golden"][n])) for n, v in zip(names, out))
-    print(f"L4 mixed: max abs err {err:.2e} (scale {scale:.2e})")
+    rel = corr_rel_err(out, np.stack([l4["golden"][n] for n in names]))
+    print(f"L4 mixed: max abs err {err:.2e} (scale {scale:.2e}), "
+          f"max per-correlator rel err {rel:.2e}")
     assert err < REL_MIXED_CORR * scale
+    assert rel < REL_MIXED_CORR
 
 
 def _vdv_columns_hp(V, phase, cols):
@@ -362,7 +371,7 @@ def test_displaced_operators_match_oracle(oracle_lib, tmp_path, precision):
     ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     out = eng.contract(gd.plan_ptr, precision, 0)
-    assert rel_err(out, ref) < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
+    assert corr_rel_err(out, ref) < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
 
 
 def _hyp_error(eng, U_ref):
@@ -445,7 +454,7 @@ def test_displaced_operators_with_smeared_links_match_oracle(oracle_lib, tmp_pat
             assert rel_err(fac.return_vdaggerv(op, t), vdv[op, t].T) < 1e-12
     ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
-    assert rel_err(eng.contract(gd.plan_ptr, precision, 0), ref) < (
+    assert corr_rel_err(eng.contract(gd.plan_ptr, precision, 0), ref) < (
         REL_FP64 if precision == 0 else REL_MIXED_CORR)
 
 
@@ -567,7 +576,7 @@ def test_vdaggerv_read_files_match_oracle(oracle_lib, tmp_path, liuming):
             assert np.array_equal(fac.return_vdaggerv(o, t), vdv[o, t].T)
     ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, Lt)
-    assert rel_err(eng.contract(gd.plan_ptr, 0, 0), ref) < REL_FP64
+    assert corr_rel_err(eng.contract(gd.plan_ptr, 0, 0), ref) < REL_FP64
 
 
 def test_vdaggerv_read_missing_files(tmp_path):
@@ -621,7 +630,7 @@ def test_pipi_kk_displaced_smeared_two_flavours_match_oracle(oracle_lib, tmp_pat
         fac.set_gauge_field(U)
         fac.create_operators(precision)
         out = eng.contract(gd.plan_ptr, precision, 0)
-        err = rel_err(out, ref)
+        err = corr_rel_err(out, ref)
         print(f"pipi + KK + displaced, smeared, two flavours: precision {precision} "
               f"max rel err {err:.2e} over {ref.shape[0]} correlators")
         assert err < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
@@ -658,7 +667,7 @@ def test_uneven_configurations_in_one_process_match_oracle(oracle_lib, tmp_path)
             eng.vdaggerv_build(precision)
         outs = [eng.contract(gd.plan_ptr, precision, 0) for gd, eng, _ in reversed(cases)]
         for (gd, eng, ref), out in zip(cases, reversed(outs)):
-            err = rel_err(out, ref)
+            err = corr_rel_err(out, ref)
             print(f"uneven {tuple(gd.dims.__getattribute__(k) for k in ('Lx', 'Lt', 'nev', 'n_rnd', 'dilT', 'dilE'))}"
                   f" precision {precision}: max rel err {err:.2e}")
             assert err < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
@@ -698,14 +707,18 @@ def test_c_caller_writes_the_reference_goldens(l4, tmp_path, precision):
     assert run.returncode == 0, run.stderr
     golden = l4["golden"]
     scale = max(float(np.max(np.abs(v))) for v in golden.values())
-    n, worst = 0, 0.0
+    n, worst, got = 0, 0.0, {}
     for f in sorted(out.glob("*.h5")):
         for name, val in read_correlators(f).items():
             worst = max(worst, float(np.max(np.abs(val - golden[name]))))
+            got[name] = val
             n += 1
-    print(f"C caller, precision {precision}: {n} datasets, max |C - golden| {worst:.2e}")
+    rel = corr_rel_err(np.stack([got[k] for k in golden]), np.stack(list(golden.values())))
+    print(f"C caller, precision {precision}: {n} datasets, max |C - golden| {worst:.2e}, "
+          f"max per-correlator rel err {rel:.2e}")
     assert n == len(golden) == 2307
     assert worst < (1e-12 if precision == 0 else 1e-10 * scale)
+    assert rel < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
 
 
 # ---------------------------------------------------------------- the command line
@@ -729,15 +742,18 @@ def test_command_line_reproduces_the_reference_goldens(l4, tmp_path, precision):
     golden = l4["golden"]
     scale = max(float(np.max(np.abs(v))) for v in golden.values())
     files = sorted((tmp_path / "correlators").glob("*_cnfg1000.h5"))
-    n, worst = 0, 0.0
+    n, worst, got = 0, 0.0, {}
     for f in files:
         for name, val in read_correlators(f).items():
             worst = max(worst, float(np.max(np.abs(val - golden[name]))))
+            got[name] = val
             n += 1
+    rel = corr_rel_err(np.stack([got[k] for k in golden]), np.stack(list(golden.values())))
     print(f"command line, {precision}: {len(files)} files, {n} datasets, "
-          f"max |output - golden| {worst:.2e}")
+          f"max |output - golden| {worst:.2e}, max per-correlator rel err {rel:.2e}")
     assert len(files) == 18 and n == len(golden) == 2307
     assert worst < (1e-12 if precision == "fp64" else 1e-10 * scale)
+    assert rel < (REL_FP64 if precision == "fp64" else REL_MIXED_CORR)
 
 
 def test_command_line_displaced_operators_smeared_links_match_oracle(oracle_lib, tmp_path):
@@ -777,7 +793,7 @@ def test_command_line_displaced_operators_smeared_links_match_oracle(oracle_lib,
     for f in (tmp_path / "correlators").glob("*_cnfg0001.h5"):
         got.update(read_correlators(f))
     assert set(got) == set(expect)
-    err = max(float(np.max(np.abs(got[k] - expect[k]))) for k in expect) / np.max(np.abs(ref))
+    err = corr_rel_err(np.stack([got[k] for k in expect]), np.stack([expect[k] for k in expect]))
     print(f"command line, displaced + smeared: {len(got)} datasets, max rel err {err:.2e}")
     assert err < REL_MIXED_CORR
 
@@ -799,3 +815,4 @@ def test_bounded_device_wait_gives_up_and_the_context_stays_usable(l4):
     golden = l4["golden"]
     names = [n for _, ds in l4["gd"].output_layout() for n in ds]
     assert max(float(np.max(np.abs(v - golden[n]))) for n, v in zip(names, out)) < 1e-10
+    assert corr_rel_err(out, np.stack([golden[n] for n in names])) < REL_MIXED_CORR

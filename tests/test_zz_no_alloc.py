@@ -93,3 +93,8 @@ def test_noalloc_vdaggerv_rejects_volumes_beyond_the_scratch(engine_lib):
     rc = fn(C.byref(dims), C.c_void_p(16), mom, C.c_void_p(16), None)
     assert rc == SLAPH_ERR_ARG
     assert b"exceeds the static scratch limit" in engine_lib.slaph_last_error()
+    # extents whose product wraps around 2^64 (2^22 each: 2^66) are refused too
+    big = Dims(1, 1 << 22, 1 << 22, 1 << 22, 8, 1, 1, 1)
+    rc = fn(C.byref(big), C.c_void_p(16), mom, C.c_void_p(16), None)
+    assert rc == SLAPH_ERR_ARG
+    assert b"exceeds the static scratch limit" in engine_lib.slaph_last_error()
