@@ -61,6 +61,16 @@ def per_correlator_rel_err(out, ref):
     return float(np.max(rel)) if rel.size else 0.0
 
 
+def workload_config(w, n_correlators, single_block_pair, world):
+    """The workload's description, printed identically by both arms."""
+    return {"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev,
+            "n_rnd": w.n_rnd, "dilution": f"TB{w.dilT} EI{w.dilE} DF4",
+            "diagrams": sorted({c.split(':')[0] for c in w.correlators}),
+            "n_correlators": int(n_correlators), "single_block_pair": single_block_pair,
+            "l2": "inputs larger than L2 (eigenvectors alone exceed 129 MB)",
+            "parallelism": f"replicas x{world}"}
+
+
 def load_peaks():
     try:
         return json.loads((REPO / "MEASURED_PEAKS.json").read_text())
@@ -390,13 +400,8 @@ def run_engine(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if precision == 0 else "bf16x6-split+f32x2+f64", "data": "synthetic",
-        "config": {"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev,
-                   "n_rnd": w.n_rnd, "dilution": f"TB{w.dilT} EI{w.dilE} DF4",
-                   "diagrams": sorted({c.split(':')[0] for c in w.correlators}),
-                   "n_correlators": int(out.shape[0]), "precision": args.precision,
-                   "single_block_pair": args.single_block_pair,
-                   "l2": "inputs larger than L2 (eigenvectors alone exceed 129 MB)",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(w, out.shape[0], args.single_block_pair, world),
+        "precision": args.precision,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "host_buffers": ("page-locked (slaph_host_alloc)" if args.host_buffers == "pinned"
@@ -422,7 +427,7 @@ def run_engine(args):
         line["fp64_value"] = fp64["value"]
         line["max_rel_err_vs_fp64"] = fp64["max_rel_err_vs_fp64"]
     if rank == 0 and not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(w, gd, args)
+        line["cpu_baseline"] = cpu_baseline(w, args)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -505,35 +510,69 @@ class CpuSample:
         }
 
 
-def cpu_baseline(w, gd, args):
-    return CpuSample(w, gd).run()
+def oracle_global_data(w):
+    """The oracle's own parse of the workload infile (no engine library)."""
+    from oracle import frontend
+    return frontend.GlobalData(w.write_infile())
+
+
+def cpu_baseline(w, args):
+    return CpuSample(w, oracle_global_data(w)).run()
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: the oracle (its CPU
+    restatement, OpenMP as the reference), with the oracle's own front end, so
+    that no engine code is loaded.  Every timed step is one bounded sample of
+    the configuration (CpuSample.run); the line's ms_per_step is that sample's
+    wall time and value the configuration time it extrapolates to, the factor
+    between them given in "extrapolation"."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300 import synthetic
     w = synthetic.CONFIGS[args.workload]
-    gd = GlobalData.from_infile(w.write_infile())
+    gd = oracle_global_data(w)
     cs = CpuSample(w, gd)
     for _ in range(args.warmup):
         cs.vdaggerv()  # untimed warm-up: page in the inputs, start the thread pool
-    vals, cb = [], None
+    vals, walls, cb = [], [], None
+    t0 = time.time()
     for _ in range(args.steps):
         cb = cs.run()
         vals.append(cb["value"])
+        walls.append(cb["sample_wall_s"])
+    timed = time.time() - t0
     v = float(np.mean(vals)) if vals else None
+    ms = 1e3 * float(np.mean(walls)) if walls else None
     if cb is not None:
         cb["value"] = v
+        cb["sample_wall_s"] = ms / 1e3
+    maps = ""
+    try:
+        maps = Path("/proc/self/maps").read_text()
+    except OSError:
+        pass
     print(json.dumps({
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": v * 1e3 if v else None, "higher_is_better": False,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev,
-                   "n_rnd": w.n_rnd, "dilution": f"TB{w.dilT} EI{w.dilE} DF4",
-                   "diagrams": sorted({c.split(':')[0] for c in w.correlators})},
+        "config": workload_config(w, gd.output_doubles() // (2 * w.Lt), args.single_block_pair,
+                                  world),
+        "timed_region_s": timed,
+        "extrapolation": {
+            "factor": v / (ms / 1e3) if v and ms else None,
+            "model": ("value = VdaggerV wave time x operators x timeslice waves + the "
+                      "dynamic schedule over the host threads of, per block pair, one cold "
+                      "slice pair + (slice pairs - 1) x one steady slice pair; "
+                      "ms_per_step is the wall time of that sample"),
+            "hook": ("one block pair per thread, as the reference's "
+                     "--single_time_slice_combination (src/global_data.cpp:84-87, "
+                     "src/Correlators.cpp:88-90) restricts contract() to one block pair, "
+                     "sampled here by one slice pair of each")},
+        "engine_library_loaded": "libslaph_gb300" in maps,
         "cpu_baseline": cb,
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))

@@ -32,6 +32,8 @@ def lib():
         L.oracle_vdaggerv_gauge.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                             C.POINTER(_dp), C.POINTER(_dp), C.POINTER(C.c_int),
                                             C.c_int, _dp]
+        L.oracle_vdaggerv_columns_dd.argtypes = [C.c_void_p, C.POINTER(C.c_int), _dp,
+                                                 C.POINTER(C.c_int), C.c_int, _dp]
         L.oracle_smear_hyp.argtypes = [C.c_void_p, C.POINTER(_dp), C.c_double, C.c_double,
                                        C.c_int]
         L.oracle_contract.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp, C.c_int,
@@ -110,6 +112,16 @@ def vdaggerv(dims, plan, V, ts=None, n_ops=None, U=None):
         uptrs = (_dp * dims.Lt)(*[_p(u) if u is not None else _dp() for u in U])
         _check(lib().oracle_vdaggerv_gauge(C.byref(dims), plan.vdv_ops, n_ops,
                                            plan.index_of_unity, ptrs, uptrs, tsp, nts, _p(out)))
+    return out
+
+
+def vdaggerv_columns_dd(dims, momentum, Vt, cols):
+    """Columns `cols` of V_t^H diag(exp(-ipx)) V_t in double-double arithmetic;
+    Vt as vdaggerv takes it.  Returns complex [len(cols)][nev]."""
+    Vt = np.ascontiguousarray(Vt, dtype=np.complex128)
+    out = np.zeros((len(cols), dims.nev), np.complex128)
+    _check(lib().oracle_vdaggerv_columns_dd(C.byref(dims), (C.c_int * 3)(*momentum), _p(Vt),
+                                            (C.c_int * len(cols))(*cols), len(cols), _p(out)))
     return out
 
 

@@ -18,7 +18,9 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 LIB = OUT / "liboracle.so"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path("/root/reference")
+# The reference source tree: $SLAPH_REFERENCE_DIR, else a directory named
+# "reference" beside this repository's root.
+REFERENCE = Path(os.environ.get("SLAPH_REFERENCE_DIR", str(HERE.parent.parent / "reference")))
 
 
 def build() -> Path:

@@ -1121,6 +1121,78 @@ int oracle_smear_hyp(const slaph_dims *dims, double *const *U, double alpha1, do
   });
 }
 
+int oracle_vdaggerv_columns_dd(const slaph_dims *dims, const int p[3], const double *Vt,
+                               const int *cols, int n_cols, double *out) {
+  return guarded([&] {
+    check_dims(dims);
+    int const nev = dims->nev;
+    long const vol = static_cast<long>(dims->Lx) * dims->Ly * dims->Lz;
+    long const dim_row = 3 * vol;
+    std::vector<cd> mom(vol);
+    create_momentum(dims->Lx, dims->Ly, dims->Lz, p, mom.data());
+    cd const *V = reinterpret_cast<cd const *>(Vt);
+    // Error-free transformations: a b = p + e exactly (fma), a + b = s + e
+    // exactly (Knuth); a double-double value is hi + lo with |lo| <= ulp(hi)/2.
+    auto two_prod = [](double a, double b, double &e) {
+      double const q = a * b;
+      e = std::fma(a, b, -q);
+      return q;
+    };
+    auto two_sum = [](double a, double b, double &e) {
+      double const s = a + b, bb = s - a;
+      e = (a - (s - bb)) + (b - bb);
+      return s;
+    };
+    struct DD {
+      double hi = 0, lo = 0;
+    };
+    auto dd_add = [&](DD x, double h, double l) {  // x + (h + l)
+      double e;
+      double const s = two_sum(x.hi, h, e);
+      e += x.lo + l;
+      DD r;
+      r.hi = s + e;
+      r.lo = e - (r.hi - s);
+      return r;
+    };
+    for (int c = 0; c < n_cols; ++c) {
+      int const j = cols[c];
+      if (j < 0 || j >= nev) throw std::runtime_error("column out of range");
+      // w = diag(mom) V_j in double-double: w_x = (wr + wrl) + i (wi + wil)
+      std::vector<double> wr(dim_row), wrl(dim_row), wi(dim_row), wil(dim_row);
+      for (long x = 0; x < dim_row; ++x) {
+        cd const m = mom[x / 3], v = V[x + dim_row * j];
+        double e1, e2, e3, e4;
+        double const a = two_prod(m.real(), v.real(), e1), b = two_prod(m.imag(), v.imag(), e2);
+        double const c1 = two_prod(m.real(), v.imag(), e3), d = two_prod(m.imag(), v.real(), e4);
+        DD r = dd_add(DD{a, e1}, -b, -e2), i = dd_add(DD{c1, e3}, d, e4);
+        wr[x] = r.hi;
+        wrl[x] = r.lo;
+        wi[x] = i.hi;
+        wil[x] = i.lo;
+      }
+#pragma omp parallel for schedule(dynamic) num_threads(oracle_threads())
+      for (int i = 0; i < nev; ++i) {
+        DD re, im;  // sum_x conj(V(x, i)) w_x
+        for (long x = 0; x < dim_row; ++x) {
+          cd const v = V[x + dim_row * i];
+          double e;
+          double h = two_prod(v.real(), wr[x], e);
+          re = dd_add(re, h, e + v.real() * wrl[x]);
+          h = two_prod(v.imag(), wi[x], e);
+          re = dd_add(re, h, e + v.imag() * wil[x]);
+          h = two_prod(v.real(), wi[x], e);
+          im = dd_add(im, h, e + v.real() * wil[x]);
+          h = two_prod(v.imag(), wr[x], e);
+          im = dd_add(im, -h, -e - v.imag() * wrl[x]);
+        }
+        out[2 * (static_cast<long>(c) * nev + i)] = re.hi + re.lo;
+        out[2 * (static_cast<long>(c) * nev + i) + 1] = im.hi + im.lo;
+      }
+    }
+  });
+}
+
 int oracle_vdaggerv_gauge(const slaph_dims *dims, const slaph_vdv_op *ops, int n_ops,
                           int index_of_unity, const double *const *V, const double *const *U,
                           const int *ts, int n_ts, double *out) {

@@ -58,6 +58,14 @@ int oracle_vdaggerv_gauge(const slaph_dims *dims, const slaph_vdv_op *ops, int n
                           int index_of_unity, const double *const *V, const double *const *U,
                           const int *ts, int n_ts, double *out);
 
+/* Columns cols[0..n_cols) of V_t^H diag(exp(-ipx)) V_t (the VdaggerV product
+ * of src/OperatorFactory.cpp:292-300) in double-double arithmetic (error-free
+ * products by fma, two-sum accumulation), a reference far more accurate than
+ * FP64 for checking large-K VdaggerV blocks.  Vt: 2*3L^3*nev doubles
+ * (column-major); out: [n_cols][nev][2]. */
+int oracle_vdaggerv_columns_dd(const slaph_dims *dims, const int p[3], const double *Vt,
+                               const int *cols, int n_cols, double *out);
+
 /* GaugeField::smearing_hyp (src/GaugeField.cpp:322-427) of every timeslice,
  * in place on U[t] (layout as above), with proj_to_su3_imp (:203-210) taking
  * (M^H M)^(-1/2) from a Jacobi eigen-decomposition. */

@@ -52,7 +52,9 @@ class GlobalData:
         argv = (C.c_char_p * max(1, len(args)))(*[a.encode() for a in args])
         h = C.c_void_p()
         L.check(L.lib().slaph_frontend_create(str(path).encode(), len(args), argv, C.byref(h)))
-        return cls(h)
+        gd = cls(h)
+        gd.infile, gd.args = str(path), list(args)
+        return gd
 
     def close(self):
         if self._h:

@@ -76,6 +76,20 @@ def l4(engine_lib):
     }
 
 
+_ORACLE_GD = {}
+
+
+def og(gd):
+    """The oracle's own parse of the infile that the engine-side GlobalData gd
+    was read from (oracle/frontend.py, independent of the engine's front end):
+    the oracle is always handed these lookup tables, never the engine's."""
+    from oracle import frontend
+    key = (gd.infile, tuple(gd.args), Path(gd.infile).read_text())
+    if key not in _ORACLE_GD:
+        _ORACLE_GD[key] = frontend.GlobalData(gd.infile, gd.args)
+    return _ORACLE_GD[key]
+
+
 def corr_rel_err(out, ref):
     """Largest relative error over correlators.  Each correlator (one row of
     Lt values, one HDF5 dataset of Diagram::write, src/Diagram.cpp:132-147) is

@@ -28,6 +28,7 @@ Run:  python tests/golden/make_l4_fixtures.py [/path/to/reference] [--only gauge
 """
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -114,7 +115,10 @@ def main(ref_root: Path):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    root = Path(args[0]) if args else Path("/root/reference")
+    # the reference tree: first argument, else $SLAPH_REFERENCE_DIR, else a
+    # directory named "reference" beside this repository's root
+    root = Path(args[0] if args else os.environ.get(
+        "SLAPH_REFERENCE_DIR", str(Path(__file__).resolve().parents[3] / "reference")))
     if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "gauge":
         write_gauge(root)
     else:

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import workload_inputs
+from conftest import workload_inputs, og
 
 
 def _blocks_from_text(text):
@@ -38,7 +38,7 @@ def test_sample_extrapolation_is_a_lower_bound(engine_lib, oracle_lib):
     gd = GlobalData.from_infile(w.write_infile())
     d = gd.dims
     V, peram, noise = workload_inputs(w)
-    vdv = oracle.vdaggerv(d, gd.plan, V)
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V)
     threads = oracle.threads()
     oracle.set_threads(1)
     # best of three of each, so that load from other processes does not decide
@@ -46,9 +46,9 @@ def test_sample_extrapolation_is_a_lower_bound(engine_lib, oracle_lib):
     try:
         for _ in range(3):
             t0 = time.perf_counter()
-            oracle.contract(d, gd.plan_ptr, vdv, peram, noise, 0, 1, gd.output_doubles())
+            oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, 1, gd.output_doubles())
             full = min(full, time.perf_counter() - t0)
-            c, st = oracle.contract_sample(d, gd.plan_ptr, vdv, peram, noise, [1])
+            c, st = oracle.contract_sample(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, [1])
             cold, steady = min(cold, c[0]), min(steady, st[0])
     finally:
         oracle.set_threads(threads)

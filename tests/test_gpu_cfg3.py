@@ -2,9 +2,15 @@
 (C2c, C3c, C4cB, C4cD, C4cV), 5 random vectors, dilution TB16 EI8 DF4.
 
 * VdaggerV (src/OperatorFactory.cpp:220-326, K = 3 * 32^3 = 98304): the FP64
-  path against the oracle on the first and last timeslice for every operator,
-  and the split-precision path against the FP64 path on every operator and
-  timeslice (relative to each block's largest entry).
+  path and the split-precision path against the oracle's double-double
+  columns (error-free products and sums, far below FP64 rounding) on three
+  columns of every operator on the first and last timeslice, each error
+  relative to the block's largest entry; the FP64 path against the oracle's
+  FP64 blocks on those timeslices, and the split-precision path against the
+  FP64 path on every operator and timeslice.  At this K two FP64 summation
+  orders differ by about 1e-12 of a block's largest entry (each rounds at that
+  level), so those two comparisons are bounded by twice the 1e-12 accuracy
+  bound that the double-double comparison asserts for each path.
 * Correlators (src/Correlators.cpp:40-127, one dataset per request,
   src/Diagram.cpp:132-147): the split-precision path against the FP64 path on
   one block pair (the reference's --single_time_slice_combination hook,
@@ -19,12 +25,12 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import corr_rel_err
+from conftest import corr_rel_err, og
 
 pytestmark = pytest.mark.gpu
 
-REL_FP64 = 1e-12
-REL_MIXED_VDV = 1e-12
+REL_VDV = 1e-12         # each path against the double-double reference
+REL_VDV_PAIR = 2e-12    # two FP64-accurate results against each other
 REL_MIXED_CORR = 1e-10
 BLOCK_PAIR = 1  # source block 0, sink block 1: 512 slice pairs
 
@@ -49,9 +55,24 @@ def test_cfg3_vdaggerv_and_correlators_mixed_vs_fp64(oracle_lib):
         eng.set_perambulator(r, w.perambulator(r))
         eng.set_random_vector(r, w.noise(r))
 
+    # double-double reference columns of every computed operator
+    ops = [o for o in range(plan.n_vdv_ops) if o != plan.index_of_unity]
+    samples = [(o, t) for o in ops for t in sample_t]
+    cols = (0, w.nev // 2, w.nev - 1)
+    ext = {}
+    for o, t in samples:
+        ref_cols = oracle.vdaggerv_columns_dd(og(gd).dims, tuple(plan.vdv_ops[o].momentum), V[t],
+                                              list(cols))
+        for c, j in enumerate(cols):
+            ext[o, t, j] = ref_cols[c]
+
+    def ext_err(blocks):
+        return max(float(np.max(np.abs(blocks[o, t][:, j] - ext[o, t, j])) /
+                         np.max(np.abs(blocks[o, t]))) for o, t, j in ext)
+
     # FP64 VdaggerV against the oracle on two timeslices
     eng.vdaggerv_build(0)
-    ref = oracle.vdaggerv(gd.dims, plan, [V.get(t) for t in range(Lt)], ts=list(sample_t))
+    ref = oracle.vdaggerv(og(gd).dims, og(gd).plan, [V.get(t) for t in range(Lt)], ts=list(sample_t))
     e_oracle = 0.0
     for op in range(plan.n_vdv_ops):
         for t in sample_t:
@@ -61,25 +82,32 @@ def test_cfg3_vdaggerv_and_correlators_mixed_vs_fp64(oracle_lib):
     del ref
     fp64 = {(op, t): eng.vdaggerv_fetch(op, t) for op in range(plan.n_vdv_ops)
             for t in range(Lt)}
+    e_fp64_ext = ext_err(fp64)
     out64 = eng.contract(gd.plan_ptr, 0, 0, single_block_pair=BLOCK_PAIR)
 
     # split precision against FP64
     eng.vdaggerv_build(1)
-    e_vdv = 0.0
+    e_vdv, mixed = 0.0, {}
     for (op, t), blk in fp64.items():
         got = eng.vdaggerv_fetch(op, t)
+        if (op, t) in samples:
+            mixed[op, t] = got
         e_vdv = max(e_vdv, float(np.max(np.abs(got - blk)) / np.max(np.abs(blk))))
+    e_mixed_ext = ext_err(mixed)
     del fp64
     outmx = eng.contract(gd.plan_ptr, 1, 0, single_block_pair=BLOCK_PAIR)
     nz = np.max(np.abs(out64), axis=1) > 0
     e_corr = corr_rel_err(outmx[nz], out64[nz])
     # correlators without a contribution from this block pair stay exactly zero
     assert np.all(outmx[~nz] == 0)
-    print(f"32^3x64: FP64 VdaggerV vs oracle {e_oracle:.2e} (t = {sample_t}); mixed "
-          f"VdaggerV vs FP64 {e_vdv:.2e} ({plan.n_vdv_ops} operators x {Lt} timeslices); "
-          f"mixed correlators vs FP64, block pair {BLOCK_PAIR}: {e_corr:.2e} per correlator "
-          f"over {int(nz.sum())} of {out64.shape[0]} correlators")
-    assert e_oracle < REL_FP64
-    assert e_vdv < REL_MIXED_VDV
+    print(f"32^3x64 VdaggerV vs double-double reference ({len(ext)} columns): FP64 "
+          f"{e_fp64_ext:.2e}, mixed {e_mixed_ext:.2e}; FP64 vs oracle {e_oracle:.2e} "
+          f"(t = {sample_t}); mixed vs FP64 {e_vdv:.2e} ({plan.n_vdv_ops} operators x {Lt} "
+          f"timeslices); mixed correlators vs FP64, block pair {BLOCK_PAIR}: {e_corr:.2e} "
+          f"per correlator over {int(nz.sum())} of {out64.shape[0]} correlators")
+    assert e_fp64_ext < REL_VDV
+    assert e_mixed_ext < REL_VDV
+    assert e_oracle < REL_VDV_PAIR
+    assert e_vdv < REL_VDV_PAIR
     assert int(nz.sum()) > 0.9 * out64.shape[0]
     assert e_corr < REL_MIXED_CORR

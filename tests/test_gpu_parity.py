@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import corr_rel_err, workload_inputs
+from conftest import corr_rel_err, workload_inputs, og
 
 pytestmark = pytest.mark.gpu
 
@@ -47,7 +47,7 @@ def l4_engine(l4):
 
 def test_vdaggerv_fp64_matches_oracle_l4(l4, l4_engine, oracle_lib):
     gd = l4["gd"]
-    ref = oracle.vdaggerv(gd.dims, gd.plan, l4["V"])  # [op][t][j][i]
+    ref = oracle.vdaggerv(og(gd).dims, og(gd).plan, l4["V"])  # [op][t][j][i]
     for op in range(gd.plan.n_vdv_ops):
         for t in range(gd.dims.Lt):
             got = l4_engine.vdaggerv_fetch(op, t)
@@ -67,8 +67,8 @@ def test_contract_fp64_reproduces_l4_goldens(l4, l4_engine, accumulator):
 
 def test_contract_fp64_matches_oracle_l4(l4, l4_engine, oracle_lib):
     gd = l4["gd"]
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, l4["V"])
-    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, l4["peram"], l4["noise"], 0, -1,
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, l4["V"])
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, l4["peram"], l4["noise"], 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     out = l4_engine.contract(gd.plan_ptr, 0, 0)
     assert np.max(np.abs(out - ref)) < 1e-13
@@ -77,9 +77,9 @@ def test_contract_fp64_matches_oracle_l4(l4, l4_engine, oracle_lib):
 
 def test_single_block_pair_l4(l4, l4_engine, oracle_lib):
     gd = l4["gd"]
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, l4["V"])
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, l4["V"])
     for b in range(3):
-        ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, l4["peram"], l4["noise"], 0, b,
+        ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, l4["peram"], l4["noise"], 0, b,
                               gd.output_doubles()).reshape(-1, gd.dims.Lt)
         out = l4_engine.contract(gd.plan_ptr, 0, 0, single_block_pair=b)
         assert np.max(np.abs(out - ref)) < 1e-13
@@ -99,12 +99,12 @@ def test_contract_fp64_matches_oracle_synthetic(name, oracle_lib):
     gd, V, peram, noise = _synthetic_case(w)
     eng = make_engine(gd, V, peram, noise)
     eng.vdaggerv_build(0)
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V)
     for op in range(gd.plan.n_vdv_ops):
         for t in (0, gd.dims.Lt - 1):
             assert rel_err(eng.vdaggerv_fetch(op, t), vdv[op, t].T) < REL_FP64
     for acc in (0, 1):
-        ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, acc, -1,
+        ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, acc, -1,
                               gd.output_doubles()).reshape(-1, gd.dims.Lt)
         out = eng.contract(gd.plan_ptr, 0, acc)
         assert corr_rel_err(out, ref) < REL_FP64
@@ -120,9 +120,9 @@ def test_two_random_vectors_raise_the_reference_error(oracle_lib):
         eng.contract(gd.plan_ptr, 0, 0)
     assert ei.value.code == SLAPH_ERR_EMPTY
     assert "inner_product" in str(ei.value)
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V)
     with pytest.raises(oracle.OracleError, match="inner_product"):
-        oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1, gd.output_doubles())
+        oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1, gd.output_doubles())
 
 
 def test_contract_before_vdaggerv_is_a_state_error(l4):
@@ -153,7 +153,7 @@ def test_vdaggerv_fp64_cfg2_full_volume(oracle_lib):
     eng.vdaggerv_build(0)
     n_ops = gd.plan.n_vdv_ops
     assert n_ops == 14  # 27 momenta merged by +-p: 13 computed + identity
-    ref = oracle.vdaggerv(gd.dims, gd.plan, [V.get(t) for t in range(w.Lt)], ts=[0, 47])
+    ref = oracle.vdaggerv(og(gd).dims, og(gd).plan, [V.get(t) for t in range(w.Lt)], ts=[0, 47])
     for op in range(n_ops):
         for t in (0, 47):
             assert rel_err(eng.vdaggerv_fetch(op, t), ref[op, t].T) < REL_FP64
@@ -186,8 +186,8 @@ def test_vdaggerv_mixed_matches_fp64_and_contract(name, oracle_lib):
         worst = max(worst, rel_err(eng.vdaggerv_fetch(op, t), ref))
     print(f"{name}: mixed VdaggerV max rel err {worst:.2e}")
     assert worst < REL_MIXED_VDV
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
-    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V)
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     out = eng.contract(gd.plan_ptr, 1, 0)
     e = corr_rel_err(out, ref)
@@ -204,8 +204,8 @@ def test_dense_trace_groups_match_oracle(name, oracle_lib):
     w = synthetic.CONFIGS[name]
     gd, V, peram, noise = _synthetic_case(w)
     eng = make_engine(gd, V, peram, noise)
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
-    refs = {acc: oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, acc, -1,
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V)
+    refs = {acc: oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, acc, -1,
                                  gd.output_doubles()).reshape(-1, gd.dims.Lt)
             for acc in (0, 1)}
     eng.vdaggerv_build(0)
@@ -364,11 +364,11 @@ def test_displaced_operators_match_oracle(oracle_lib, tmp_path, precision):
     for t, u in enumerate(U):
         eng.set_gauge(t, u)
     eng.vdaggerv_build(precision)
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=U)
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V, U=U)
     for op in range(gd.plan.n_vdv_ops):
         for t in range(gd.dims.Lt):
             assert rel_err(eng.vdaggerv_fetch(op, t), vdv[op, t].T) < 1e-12
-    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     out = eng.contract(gd.plan_ptr, precision, 0)
     assert corr_rel_err(out, ref) < (REL_FP64 if precision == 0 else REL_MIXED_CORR)
@@ -419,11 +419,11 @@ def test_hyp_smearing_matches_oracle(oracle_lib, tmp_path):
         for t, u in enumerate(U):
             eng.set_gauge(t, u)
         eng.smear_gauge_hyp(0.75, 0.6, iters)
-        err = _hyp_error(eng, oracle.smear_hyp(gd.dims, U, 0.75, 0.6, iters))
+        err = _hyp_error(eng, oracle.smear_hyp(og(gd).dims, U, 0.75, 0.6, iters))
         print(f"HYP {L}^3 x {Lt}, {iters} iterations: max |device - oracle| {err:.2e}")
         assert err < 1e-12
         eng.smear_gauge_hyp(0.75, 0.6, 0)  # no iterations: unchanged
-        assert _hyp_error(eng, oracle.smear_hyp(gd.dims, U, 0.75, 0.6, iters)) < 1e-12
+        assert _hyp_error(eng, oracle.smear_hyp(og(gd).dims, U, 0.75, 0.6, iters)) < 1e-12
 
 
 @pytest.mark.parametrize("precision", [0, 1])
@@ -447,12 +447,12 @@ def test_displaced_operators_with_smeared_links_match_oracle(oracle_lib, tmp_pat
     fac = OperatorFactory(eng, gd)
     fac.set_gauge_field(U)
     fac.create_operators(precision)
-    S = oracle.smear_hyp(gd.dims, U, 0.62, 0.62, 3)
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=S)
+    S = oracle.smear_hyp(og(gd).dims, U, 0.62, 0.62, 3)
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V, U=S)
     for op in range(gd.plan.n_vdv_ops):
         for t in range(gd.dims.Lt):
             assert rel_err(fac.return_vdaggerv(op, t), vdv[op, t].T) < 1e-12
-    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     assert corr_rel_err(eng.contract(gd.plan_ptr, precision, 0), ref) < (
         REL_FP64 if precision == 0 else REL_MIXED_CORR)
@@ -530,7 +530,7 @@ def test_vdaggerv_write_files(oracle_lib, tmp_path):
 
 
 def _oracle_blocks(gd, V):
-    return oracle.vdaggerv(gd.dims, gd.plan, V)  # [op][t] column-major blocks
+    return oracle.vdaggerv(og(gd).dims, og(gd).plan, V)  # [op][t] column-major blocks
 
 
 @pytest.mark.parametrize("liuming", [False, True])
@@ -574,7 +574,7 @@ def test_vdaggerv_read_files_match_oracle(oracle_lib, tmp_path, liuming):
     for o in range(gd.plan.n_vdv_ops):
         for t in range(Lt):
             assert np.array_equal(fac.return_vdaggerv(o, t), vdv[o, t].T)
-    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, Lt)
     assert corr_rel_err(eng.contract(gd.plan_ptr, 0, 0), ref) < REL_FP64
 
@@ -620,8 +620,8 @@ def test_pipi_kk_displaced_smeared_two_flavours_match_oracle(oracle_lib, tmp_pat
     V, peram, noise = workload_inputs(w)
     U = _fixture_links(4, 8, seed=9)
     a1, a2, n_hyp = gd.hyp_parameters()
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=oracle.smear_hyp(gd.dims, U, a1, a2, n_hyp))
-    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V, U=oracle.smear_hyp(og(gd).dims, U, a1, a2, n_hyp))
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     assert np.max(np.abs(ref)) > 0
     for precision in (0, 1):
@@ -658,8 +658,8 @@ def test_uneven_configurations_in_one_process_match_oracle(oracle_lib, tmp_path)
                                seed=70 + i)
         gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
         V, peram, noise = workload_inputs(w)
-        vdv = oracle.vdaggerv(gd.dims, gd.plan, V)
-        ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+        vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V)
+        ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
                               gd.output_doubles()).reshape(-1, Lt)
         cases.append((gd, make_engine(gd, V, peram, noise), ref))
     for precision in (1, 0):
@@ -785,8 +785,8 @@ def test_command_line_displaced_operators_smeared_links_match_oracle(oracle_lib,
     from slaph_gb300.frontend import read_gauge_lime
     U = [np.ascontiguousarray(u) for u in read_gauge_lime(GOLDEN / "l4" / "gauge_conf.1000",
                                                           4, 4, 4, 4, 3)]
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, V, U=oracle.smear_hyp(gd.dims, U, 0.62, 0.62, 2))
-    ref = oracle.contract(gd.dims, gd.plan_ptr, vdv, peram, noise, 0, -1,
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V, U=oracle.smear_hyp(og(gd).dims, U, 0.62, 0.62, 2))
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
                           gd.output_doubles()).reshape(-1, gd.dims.Lt)
     expect = dict(zip([n for _, ds in gd.output_layout() for n in ds], ref))
     got = {}

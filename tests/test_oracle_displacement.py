@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import og
 
 
 def neighbours(L1, L2):
@@ -67,7 +68,7 @@ def test_displaced_vdaggerv_matches_reference_loop(engine_lib, oracle_lib, tmp_p
     # [site][dir][3x3 column-major]: element (a, b) at a + 3 b
     U_cm = [np.ascontiguousarray(u.transpose(0, 1, 3, 2)) for u in U]
     V = [w.eigenvectors(t) for t in range(d.Lt)]
-    got = oracle.vdaggerv(d, gd.plan, V, U=U_cm)
+    got = oracle.vdaggerv(og(gd).dims, og(gd).plan, V, U=U_cm)
     iup, idn = neighbours(d.Lx, d.Ly)
     n_disp = 0
     for o in range(gd.plan.n_vdv_ops):

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import og
 
 TOL = 1e-12  # tests/integration-L4/compare:16
 
@@ -15,13 +16,13 @@ TOL = 1e-12  # tests/integration-L4/compare:16
 @pytest.fixture(scope="module")
 def l4_oracle(l4, oracle_lib):
     gd = l4["gd"]
-    vdv = oracle.vdaggerv(gd.dims, gd.plan, l4["V"])
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, l4["V"])
     return gd, vdv
 
 
 def _run(l4, l4_oracle, accumulator):
     gd, vdv = l4_oracle
-    out = oracle.contract(gd.dims, gd.plan_ptr, vdv, l4["peram"], l4["noise"], accumulator,
+    out = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, l4["peram"], l4["noise"], accumulator,
                           -1, gd.output_doubles())
     return out.reshape(-1, gd.dims.Lt)
 
@@ -47,7 +48,7 @@ def test_oracle_single_block_pair_sums_to_full(l4, l4_oracle):
     gd, vdv = l4_oracle
     full = _run(l4, l4_oracle, 0)
     nb = gd.dims.Lt // gd.dims.dilT
-    parts = sum(oracle.contract(gd.dims, gd.plan_ptr, vdv, l4["peram"], l4["noise"], 0, b,
+    parts = sum(oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, l4["peram"], l4["noise"], 0, b,
                                 gd.output_doubles()).reshape(-1, gd.dims.Lt)
                 for b in range(nb * (nb + 1) // 2))
     np.testing.assert_allclose(parts, full, rtol=0, atol=1e-13)
