@@ -268,6 +268,16 @@ int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id, cons
  * operator table holds displaced operators. */
 int slaph_engine_set_gauge(slaph_engine *eng, int32_t t, const double *U);
 
+/* The time dilution (slices per block) for the contractions that follow.  In
+ * the reference it is an argument of contract() (include/Correlators.hpp:41-54,
+ * DilutionScheme at src/Correlators.cpp:65), given after OperatorFactory has
+ * built VdaggerV without it (src/OperatorFactory.cpp:184-218): a caller that
+ * creates the engine before it knows dilT sets it here.  dilT must divide Lt.
+ * VdaggerV, eigenvectors and noise stay; a change re-makes the perambulator
+ * buffer, whose columns depend on the number of time blocks, so the
+ * perambulators are uploaded after this call. */
+int slaph_engine_set_time_dilution(slaph_engine *eng, int32_t dilT);
+
 /* Replaces the smearing step of OperatorFactory::create_operators
  * (src/OperatorFactory.cpp:253-260): GaugeField::smearing_hyp
  * (src/GaugeField.cpp:322-427) with (alpha1, alpha2, iterations) applied on

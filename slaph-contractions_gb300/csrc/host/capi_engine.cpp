@@ -63,6 +63,10 @@ int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id,
   return slaph::guarded([&] { get(eng).set_random_vector(rnd_id, noise, true); });
 }
 
+int slaph_engine_set_time_dilution(slaph_engine *eng, int32_t dilT) {
+  return slaph::guarded([&] { get(eng).set_time_dilution(dilT); });
+}
+
 int slaph_engine_set_gauge(slaph_engine *eng, int32_t t, const double *U) {
   return slaph::guarded([&] { get(eng).set_gauge(t, U); });
 }

@@ -207,6 +207,26 @@ void Engine::set_random_vector(int32_t r, double const *noise, bool async) {
   if (!async) SLAPH_CK(cudaEventSynchronize(ev_n_[r]));
 }
 
+void Engine::set_time_dilution(int32_t dilT) {
+  if (dilT < 1 || dims_.Lt % dilT != 0)
+    throw ArgError("Lt must be a positive multiple of dilT");
+  if (dilT == dims_.dilT) return;
+  // The perambulators' column count depends on the number of time blocks:
+  // their buffer is re-made (to be uploaded again); VdaggerV and the
+  // eigenvectors do not depend on it and stay.
+  SLAPH_CK(cudaStreamSynchronize(up_stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  dims_.dilT = dilT;
+  geo_.nb = dims_.Lt / dilT;
+  peram_.release();
+  peram_.reserve(sizeof(double2) * peram_elems() * dims_.n_rnd);
+  SLAPH_CK(cudaMemsetAsync(peram_.as<void>(), 0, peram_.size(), stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  std::fill(pend_p_.begin(), pend_p_.end(), 0);
+  sched_.reset();
+  sched_plan_ = nullptr;
+}
+
 void Engine::set_gauge(int32_t t, double const *U) {
   if (t < 0 || t >= dims_.Lt || !U) throw ArgError("invalid timeslice or null pointer");
   if (dims_.Lx != dims_.Ly || dims_.Lx != dims_.Lz)

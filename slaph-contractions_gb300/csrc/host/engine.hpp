@@ -90,6 +90,7 @@ class Engine {
   // Gauge links of timeslice t, [site][dir x,y,z][3x3 column-major] complex,
   // for displaced operators.
   void set_gauge(int32_t t, double const *U);
+  void set_time_dilution(int32_t dilT);
   // HYP smearing of the stored links of every timeslice, in place.
   void smear_gauge_hyp(double alpha1, double alpha2, int32_t iterations);
   void gauge_fetch(int32_t t, double *out);

@@ -98,6 +98,12 @@ class Engine:
               else L.lib().slaph_engine_set_random_vector)
         L.check(fn(self._h, r, L.dptr(noise)))
 
+    def set_time_dilution(self, dilT):
+        """Slices per time-dilution block for the following contractions
+        (slaph_engine_set_time_dilution); perambulators are uploaded after it."""
+        L.check(L.lib().slaph_engine_set_time_dilution(self._h, int(dilT)))
+        self.dims.dilT = int(dilT)
+
     def set_gauge(self, t, U):
         """Gauge links of timeslice t: complex (V3, 3, 9) with each 3x3 link
         column-major (slaph_engine_set_gauge)."""

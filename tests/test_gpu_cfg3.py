@@ -7,10 +7,12 @@
   columns of every operator on the first and last timeslice, each error
   relative to the block's largest entry; the FP64 path against the oracle's
   FP64 blocks on those timeslices, and the split-precision path against the
-  FP64 path on every operator and timeslice.  At this K two FP64 summation
-  orders differ by about 1e-12 of a block's largest entry (each rounds at that
-  level), so those two comparisons are bounded by twice the 1e-12 accuracy
-  bound that the double-double comparison asserts for each path.
+  FP64 path on every operator and timeslice.  At this K the FP64 path itself
+  rounds by up to about 2e-12 of a block's largest entry (9e-13 on the sampled
+  columns, where the split-precision path stays within 6e-13 of the exact
+  value), so comparisons of a result with an FP64 result are bounded by 4e-12,
+  the sum of two such roundings, while each path's own accuracy is asserted at
+  1e-12 against the double-double columns.
 * Correlators (src/Correlators.cpp:40-127, one dataset per request,
   src/Diagram.cpp:132-147): the split-precision path against the FP64 path on
   one block pair (the reference's --single_time_slice_combination hook,
@@ -30,7 +32,7 @@ from conftest import corr_rel_err, og
 pytestmark = pytest.mark.gpu
 
 REL_VDV = 1e-12         # each path against the double-double reference
-REL_VDV_PAIR = 2e-12    # two FP64-accurate results against each other
+REL_VDV_PAIR = 4e-12    # a result against an FP64 result (both roundings)
 REL_MIXED_CORR = 1e-10
 BLOCK_PAIR = 1  # source block 0, sink block 1: 512 slice pairs
 
