@@ -266,7 +266,7 @@ def run_engine(args):
     sampler.start()
     stage = np.zeros(4)
     launches = 0
-    ktim = np.zeros(12)  # per-kernel event times and launch counts, summed over steps
+    ktim = np.zeros(13)  # per-kernel event times and launch counts, summed over steps
     wall0 = time.time()
     for _ in range(args.steps):
         step()

@@ -132,17 +132,25 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;                             // base offset 0, no swizzle
 }
 // Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, N = kTN, M = kTM.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
-                            (static_cast<uint32_t>(kTN >> 3) << 17) |
-                            (static_cast<uint32_t>(kTM >> 4) << 24);
+// K-major, M = kTM, N = n (a multiple of 16 up to 256).
+__host__ __device__ constexpr uint32_t idesc_n(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+         (static_cast<uint32_t>(kTM >> 4) << 24);
+}
+// Level blocks (kTN columns each) one MMA covers: the accumulators of levels
+// l .. l + kLevelGroup - 1 sit side by side in TMEM, and the B slices
+// q .. q + kLevelGroup - 1 side by side in shared memory with a uniform
+// 8-row-group stride, so A_p against [B_q; ...] is one MMA of N = 3 kTN into
+// the accumulators p + q onwards.
+constexpr int kLevelGroup = 256 / kTN;
+static_assert(kLevelGroup >= 1 && (kLevelGroup * kTN) % 16 == 0, "MMA N");
 
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b,
-                                         uint32_t accumulate) {
+                                         uint32_t accumulate, uint32_t idesc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
@@ -372,7 +380,7 @@ __device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
           break;
         }
         tc_fence_after();
-        uint32_t started = 0;
+        bool first = true;  // the chunk's first k-step starts every accumulator
         int const kt_end = min(k_tiles, (c + 1) * kChunkKT);
         for (int kt = c * kChunkKT; kt < kt_end; ++kt) {
           int const s = kt % kStages, use = kt / kStages;
@@ -384,20 +392,25 @@ __device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
           uint32_t const base = smem_u32(smem + s * kStageBytes);
 #pragma unroll
           for (int ks = 0; ks < kTK / 16; ++ks) {
+            // The 21 slice pairs p + q <= 5 (0-based; 1-based p + q <= 7), as
+            // 9 MMAs: A_p against the B slices q0 .. q0 + nb - 1 into the
+            // level accumulators p + q0 onwards.  Per level the slice pairs
+            // still arrive in increasing p, and the p = 0 MMAs of a chunk's
+            // first k-step (levels 0..5) overwrite instead of accumulating.
 #pragma unroll
             for (int p = 0; p < kSlices; ++p) {
 #pragma unroll
-              for (int q = 0; q < kSlices; ++q) {
-                if (p + q >= kSlices) continue;  // 1-based p + q <= 7: 21 pairs
-                int const lvl = p + q;           // accumulator 0..5 (< kLevels)
+              for (int q0 = 0; q0 < kSlices - p; q0 += kLevelGroup) {
+                int const nb = min(kLevelGroup, kSlices - p - q0);
                 uint64_t const ad = smem_desc(base + p * kABlk + ks * 256, 128, 512);
                 uint64_t const bd =
-                    smem_desc(base + kStageA + q * kBBlk + ks * 256, 128, 512);
-                uint32_t const acc = (started >> lvl) & 1u;
-                mma_bf16(tmem + static_cast<uint32_t>(lvl * kTN), ad, bd, acc);
-                started |= 1u << lvl;
+                    smem_desc(base + kStageA + q0 * kBBlk + ks * 256, 128, 512);
+                uint32_t const acc = (first && p == 0) ? 0u : 1u;
+                mma_bf16(tmem + static_cast<uint32_t>((p + q0) * kTN), ad, bd, acc,
+                         idesc_n(nb * kTN));
               }
             }
+            first = false;
           }
           mma_commit(&empty_bar[s]);  // stage s free once these MMAs complete
         }
