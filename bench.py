@@ -217,14 +217,29 @@ def run_engine(args):
         return p
 
     t_gen = time.time()
-    V = [pinned_copy(w.eigenvectors(t)) for t in range(w.Lt)]
+    # Workloads with a period keep that many distinct timeslices on the host
+    # (every timeslice is still copied and computed).
+    n_distinct = w.v_period if w.v_period > 0 else w.Lt
+    pool = [pinned_copy(w.eigenvectors(t)) for t in range(n_distinct)]
+    V = [pool[t % n_distinct] for t in range(w.Lt)]
     peram = [pinned_copy(w.perambulator(r)) for r in range(w.n_rnd)]
     noise = pinned_copy(np.stack([w.noise(r) for r in range(w.n_rnd)]))
-    t_gen = time.time() - t_gen
     precision = 1 if args.precision == "mixed" else 0
 
     eng = Engine(dims)
     eng.set_operators(gd.plan)
+    slots = args.eigenvector_slots if args.eigenvector_slots >= 0 else w.eigenvector_slots
+    if slots > 0:
+        eng.set_eigenvector_slots(slots)  # streamed: the builds copy from V
+    # Displaced operators: gauge links of every timeslice, uploaded and
+    # HYP-smeared (infile alpha1, alpha2, iterations) per configuration, as
+    # create_operators reads and smears them (src/OperatorFactory.cpp:248-260).
+    U = None
+    if gd.plan.need_gaugefield:
+        upool = [pinned_copy(w.gauge_links(t)) for t in range(n_distinct)]
+        U = [upool[t % n_distinct] for t in range(w.Lt)]
+    hyp = gd.hyp_parameters()
+    t_gen = time.time() - t_gen
 
     def upload_eigenvectors(asynchronous=True):
         # Enqueued on the engine's upload stream; the VdaggerV build waits for
@@ -243,10 +258,33 @@ def run_engine(args):
         upload_eigenvectors(asynchronous)
         upload_rest(asynchronous)
 
+    def gauge():
+        # links of the configuration, smeared on the device (timings[13])
+        if U is None:
+            return 0.0
+        for t, u in enumerate(U):
+            eng.set_gauge(t, u)
+        if hyp[2] > 0:
+            eng.smear_gauge_hyp(*hyp)
+            return float(eng.timings()[13])
+        return 0.0
+
     def step():
+        gauge()
         eng.vdaggerv_build(precision)
         out = eng.contract(gd.plan_ptr, precision, 0, args.single_block_pair)
         return out
+
+    def device_memory_used():
+        import ctypes
+        try:
+            rt = ctypes.CDLL("libcudart.so")
+        except OSError:
+            return None
+        free, total = ctypes.c_size_t(), ctypes.c_size_t()
+        if rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) != 0:
+            return None
+        return (total.value - free.value) / 1e9
 
 
     t0 = time.time()
@@ -264,16 +302,23 @@ def run_engine(args):
     barrier(dist)
     sampler = ClockSampler(local)
     sampler.start()
-    stage = np.zeros(4)
+    stage = np.zeros(5)  # VdaggerV, factors, products + traces, assembly, HYP smearing
     launches = 0
-    ktim = np.zeros(13)  # per-kernel event times and launch counts, summed over steps
+    ktim = np.zeros_like(eng.timings())  # per-kernel times and launch counts, over steps
+    mem_hw = device_memory_used()
     wall0 = time.time()
     for _ in range(args.steps):
-        step()
+        h = gauge()
+        eng.vdaggerv_build(precision)
+        eng.contract(gd.plan_ptr, precision, 0, args.single_block_pair)
         tim = eng.timings()
-        stage += tim[:4]
+        stage[:4] += tim[:4]
+        stage[4] += h
         launches += int(tim[5])
         ktim += tim
+        m = device_memory_used()
+        if m is not None:
+            mem_hw = max(mem_hw or 0.0, m)
     wall = time.time() - wall0
     clocks = sampler.stop()
     dev_s = stage.sum() / 1e3 / args.steps
@@ -292,6 +337,7 @@ def run_engine(args):
     for i in range(args.steps):
         t_a = time.time()
         upload_rest()
+        gauge()
         eng.vdaggerv_build(precision)
         if i + 1 < args.steps:
             upload_eigenvectors()
@@ -299,7 +345,8 @@ def run_engine(args):
         out = eng.contract(gd.plan_ptr, precision, 0, args.single_block_pair)
         e2e_parts.append((t_b - t_a, time.time() - t_b))
     e2e = max_over_ranks(dist, (time.time() - e2e0) / args.steps)
-    h2d = sum(v.nbytes for v in V) + sum(p.nbytes for p in peram) + noise.nbytes
+    h2d = (sum(v.nbytes for v in V) + sum(p.nbytes for p in peram) + noise.nbytes
+           + (sum(u.nbytes for u in U) if U is not None else 0))
     d2h = out.nbytes
 
     # ---- the plain FP64 path on the same inputs (outside the timed regions):
@@ -313,10 +360,11 @@ def run_engine(args):
         out64 = eng.contract(gd.plan_ptr, 0, 0, args.single_block_pair)
         t_c = eng.timings()
         wall64 = time.time() - w0
-        st64 = [t_v[0], t_c[1], t_c[2], t_c[3]]
+        # the same (FP64) HYP smearing precedes both builds
+        st64 = [t_v[0], t_c[1], t_c[2], t_c[3], stage[4] / args.steps]
         fp64 = {"value": float(sum(st64)) / 1e3, "unit": UNIT,
-                "stages_ms": dict(zip(["vdaggerv", "factors", "products_traces", "assembly"],
-                                      map(float, st64))),
+                "stages_ms": dict(zip(["vdaggerv", "factors", "products_traces", "assembly",
+                                       "hyp_smearing"], map(float, st64))),
                 "wall_s": wall64,
                 "max_rel_err_vs_fp64": per_correlator_rel_err(out, out64),
                 "n_correlators": int(out64.shape[0]),
@@ -334,7 +382,7 @@ def run_engine(args):
     note = "of measured" if peaks else "of fallback"
     peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks
                 else "fallback 1.7 PFLOP/s sustained")
-    names = ["vdaggerv", "factors", "products_traces", "assembly"]
+    names = ["vdaggerv", "factors", "products_traces", "assembly", "hyp_smearing"]
     eds = 4 * w.dilE
     K = args.steps
     # Kernels timed on their own by the engine's CUDA events (per step).
@@ -417,6 +465,9 @@ def run_engine(args):
                  "product_trace_tflop": stats[5] / 1e12, "factors": stats[0],
                  "products": stats[1], "trace_entries": stats[2], "terms": stats[3]},
         "planning_s": plan_s, "first_step_s": first, "input_generation_s": t_gen,
+        "device_memory_used_gb": mem_hw,
+        "eigenvectors": (f"streamed through {slots} device slots" if slots > 0
+                         else "resident (all timeslices)"),
 
         "roofline": roofline, "roofline_others": others, "kernels_ms": kernels_ms,
         "clocks": clocks,
@@ -432,6 +483,60 @@ def run_engine(args):
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_uneven(args):
+    """The uneven batch (synthetic.UNEVEN_CFG4): six configurations of
+    different lattice size, Nev, random-vector count and time dilution, one
+    after another in one process, each through its own engine.  Per instance:
+    the split-precision time per configuration (device stage times, after one
+    warm-up configuration that plans and allocates), the plain FP64 path's
+    time, and every correlator of the split-precision result against the FP64
+    result, relative per correlator."""
+    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300.engine import Engine
+    rows = []
+    t_all = time.time()
+    for w in synthetic.UNEVEN_CFG4:
+        gd = GlobalData.from_infile(w.write_infile())
+        eng = Engine(gd.dims)
+        eng.set_operators(gd.plan)
+        for t in range(w.Lt):
+            eng.set_eigenvectors(t, w.eigenvectors(t))
+        for r in range(w.n_rnd):
+            eng.set_perambulator(r, w.perambulator(r))
+            eng.set_random_vector(r, w.noise(r))
+
+        def run(precision):
+            eng.vdaggerv_build(precision)
+            v = eng.timings()[0]
+            out = eng.contract(gd.plan_ptr, precision, 0)
+            tim = eng.timings()
+            return out, (v + tim[1] + tim[2] + tim[3]) / 1e3
+
+        run(1)  # warm-up: planning and allocations
+        secs = []
+        for _ in range(max(1, args.steps)):
+            out, sec = run(1)
+            secs.append(sec)
+        out64, sec64 = run(0)
+        rows.append({"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev,
+                     "n_rnd": w.n_rnd, "dilution": f"TB{w.dilT} EI{w.dilE} DF4",
+                     "n_correlators": int(out.shape[0]), "value": float(np.mean(secs)),
+                     "fp64_value": sec64,
+                     "max_rel_err_vs_fp64": per_correlator_rel_err(out, out64)})
+        eng.close()
+    total = sum(r["value"] for r in rows)
+    print(json.dumps({
+        "metric": "s/gauge-config, six uneven configurations (24^3x48 and 32^3x64, "
+                  "Nev 64-220), split precision vs FP64",
+        "value": total / len(rows), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "higher_is_better": False, "dtype": "bf16x6-split+f32x2+f64", "data": "synthetic",
+        "config": {"workload": "cfg4_uneven", "instances": len(rows),
+                   "order": "one after another in one process, one engine each"},
+        "sum_s": total, "fp64_sum_s": sum(r["fp64_value"] for r in rows),
+        "max_rel_err_vs_fp64": max(r["max_rel_err_vs_fp64"] for r in rows),
+        "instances": rows, "wall_s": time.time() - t_all}))
 
 
 def _dynamic_schedule(times, threads):
@@ -588,6 +693,9 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--single-block-pair", type=int, default=-1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--eigenvector-slots", type=int, default=-1,
+                    help="stream the eigenvectors through this many device slots "
+                         "(0: all resident; default: the workload's setting)")
     ap.add_argument("--no-fp64-check", action="store_true",
                     help="skip the FP64 run and the per-correlator comparison after timing")
     ap.add_argument("--host-buffers", choices=["pinned", "pageable"], default="pinned",
@@ -595,6 +703,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "cfg4_uneven":
+        run_uneven(args)
     else:
         run_engine(args)
 

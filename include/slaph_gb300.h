@@ -224,7 +224,9 @@ int slaph_write_correlators_h5(const char *file_path, int32_t n_datasets,
 typedef struct slaph_engine slaph_engine;
 
 /* Creates an engine on the current CUDA device.  Allocates the device arrays
- * for eigenvectors (all timeslices), perambulators and noise. */
+ * for perambulators and noise; the eigenvectors of all timeslices are
+ * allocated by the first slaph_engine_set_eigenvectors (or a ring of a few
+ * timeslices by slaph_engine_set_eigenvector_slots). */
 int slaph_engine_create(const slaph_dims *dims, slaph_engine **out);
 int slaph_engine_destroy(slaph_engine *eng);
 
@@ -248,6 +250,18 @@ int slaph_engine_set_operators(slaph_engine *eng, const slaph_vdv_op *ops, int32
  * slaph_vdaggerv_build, so the next configuration's eigenvectors may be
  * uploaded between a build and the contraction that follows it. */
 int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V);
+/* Eigenvectors streamed per timeslice, as the reference reads them inside its
+ * VdaggerV loop (src/OperatorFactory.cpp:263-300), for lattices whose
+ * eigenvectors do not fit on the device next to everything else (48^3 x 96,
+ * Nev 220: 112 GB).  n_slots >= 2: the engine keeps a ring of n_slots
+ * timeslices instead of all Lt; both eigenvector setters then only record the
+ * host buffer of timeslice t, and slaph_vdaggerv_build copies the timeslices
+ * n_slots / 2 at a time into one half of the ring while it computes the other,
+ * so every host buffer must stay valid and unchanged until the build returns
+ * (page-locked buffers from slaph_host_alloc copy at the full link rate).
+ * n_slots = 0 returns to all timeslices resident (the default).  Earlier
+ * eigenvector uploads and VdaggerV are discarded by a change. */
+int slaph_engine_set_eigenvector_slots(slaph_engine *eng, int32_t n_slots);
 int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram);
 int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise);
 int slaph_engine_set_eigenvectors_async(slaph_engine *eng, int32_t t, const double *V);
@@ -380,8 +394,9 @@ int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
  * its launch count, out[8] the tensor-core trace GEMM (mixed precision),
  * out[9] its launch count, out[10] the slicing of its operands, out[11] the
  * split-precision VdaggerV GEMM alone (summed over its launches; set by the
- * build), out[12] its launch count.  Returns the number of values written
- * (<= n, at most 13). */
+ * build), out[12] its launch count, out[13] the last HYP smearing
+ * (slaph_engine_smear_gauge_hyp).  Returns the number of values written
+ * (<= n, at most 14). */
 int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
 
 /* VdaggerV of one operator on one timeslice for callers that cannot let a

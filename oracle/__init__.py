@@ -34,6 +34,9 @@ def lib():
                                             C.c_int, _dp]
         L.oracle_vdaggerv_columns_dd.argtypes = [C.c_void_p, C.POINTER(C.c_int), _dp,
                                                  C.POINTER(C.c_int), C.c_int, _dp]
+        L.oracle_vdaggerv_columns_dd_w.argtypes = [C.c_void_p, _dp, _dp, C.POINTER(C.c_int),
+                                                   C.c_int, _dp]
+        L.oracle_displace_eigenvectors.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp]
         L.oracle_smear_hyp.argtypes = [C.c_void_p, C.POINTER(_dp), C.c_double, C.c_double,
                                        C.c_int]
         L.oracle_contract.argtypes = [C.c_void_p, C.c_void_p, _dp, C.POINTER(_dp), _dp, C.c_int,
@@ -122,6 +125,26 @@ def vdaggerv_columns_dd(dims, momentum, Vt, cols):
     out = np.zeros((len(cols), dims.nev), np.complex128)
     _check(lib().oracle_vdaggerv_columns_dd(C.byref(dims), (C.c_int * 3)(*momentum), _p(Vt),
                                             (C.c_int * len(cols))(*cols), len(cols), _p(out)))
+    return out
+
+
+def displace_eigenvectors(dims, op, Vt, Ut):
+    """D(V_t) of the displaced operator op (a plan's VdvOp) on links Ut."""
+    Vt = np.ascontiguousarray(Vt, dtype=np.complex128)
+    out = np.zeros_like(Vt)
+    _check(lib().oracle_displace_eigenvectors(C.byref(dims), C.byref(op), _p(Vt),
+                                              _p(np.ascontiguousarray(Ut, dtype=np.complex128)),
+                                              _p(out)))
+    return out
+
+
+def vdaggerv_columns_dd_w(dims, Vt, Wt, cols):
+    """Columns `cols` of V_t^H W in double-double arithmetic."""
+    Vt = np.ascontiguousarray(Vt, dtype=np.complex128)
+    Wt = np.ascontiguousarray(Wt, dtype=np.complex128)
+    out = np.zeros((len(cols), dims.nev), np.complex128)
+    _check(lib().oracle_vdaggerv_columns_dd_w(C.byref(dims), _p(Vt), _p(Wt),
+                                              (C.c_int * len(cols))(*cols), len(cols), _p(out)))
     return out
 
 

@@ -1121,16 +1121,20 @@ int oracle_smear_hyp(const slaph_dims *dims, double *const *U, double alpha1, do
   });
 }
 
-int oracle_vdaggerv_columns_dd(const slaph_dims *dims, const int p[3], const double *Vt,
-                               const int *cols, int n_cols, double *out) {
+namespace {
+// Columns of V^H W in double-double arithmetic, W = diag(mom) V (mom given)
+// or W given (Wd, exact double entries).
+int vdaggerv_columns_dd(const slaph_dims *dims, const int *p, const double *Vt, const double *Wd,
+                        const int *cols, int n_cols, double *out) {
   return guarded([&] {
     check_dims(dims);
     int const nev = dims->nev;
     long const vol = static_cast<long>(dims->Lx) * dims->Ly * dims->Lz;
     long const dim_row = 3 * vol;
-    std::vector<cd> mom(vol);
-    create_momentum(dims->Lx, dims->Ly, dims->Lz, p, mom.data());
+    std::vector<cd> mom(vol, cd(1.0, 0.0));
+    if (p) create_momentum(dims->Lx, dims->Ly, dims->Lz, p, mom.data());
     cd const *V = reinterpret_cast<cd const *>(Vt);
+    cd const *Wg = reinterpret_cast<cd const *>(Wd);
     // Error-free transformations: a b = p + e exactly (fma), a + b = s + e
     // exactly (Knuth); a double-double value is hi + lo with |lo| <= ulp(hi)/2.
     auto two_prod = [](double a, double b, double &e) {
@@ -1161,7 +1165,8 @@ int oracle_vdaggerv_columns_dd(const slaph_dims *dims, const int p[3], const dou
       // w = diag(mom) V_j in double-double: w_x = (wr + wrl) + i (wi + wil)
       std::vector<double> wr(dim_row), wrl(dim_row), wi(dim_row), wil(dim_row);
       for (long x = 0; x < dim_row; ++x) {
-        cd const m = mom[x / 3], v = V[x + dim_row * j];
+        cd const m = Wg ? cd(1.0, 0.0) : mom[x / 3];
+        cd const v = Wg ? Wg[x + dim_row * j] : V[x + dim_row * j];
         double e1, e2, e3, e4;
         double const a = two_prod(m.real(), v.real(), e1), b = two_prod(m.imag(), v.imag(), e2);
         double const c1 = two_prod(m.real(), v.imag(), e3), d = two_prod(m.imag(), v.real(), e4);
@@ -1190,6 +1195,34 @@ int oracle_vdaggerv_columns_dd(const slaph_dims *dims, const int p[3], const dou
         out[2 * (static_cast<long>(c) * nev + i) + 1] = im.hi + im.lo;
       }
     }
+  });
+}
+}  // namespace
+
+int oracle_vdaggerv_columns_dd(const slaph_dims *dims, const int p[3], const double *Vt,
+                               const int *cols, int n_cols, double *out) {
+  return vdaggerv_columns_dd(dims, p, Vt, nullptr, cols, n_cols, out);
+}
+
+int oracle_vdaggerv_columns_dd_w(const slaph_dims *dims, const double *Vt, const double *Wt,
+                                 const int *cols, int n_cols, double *out) {
+  return vdaggerv_columns_dd(dims, nullptr, Vt, Wt, cols, n_cols, out);
+}
+
+int oracle_displace_eigenvectors(const slaph_dims *dims, const slaph_vdv_op *op,
+                                 const double *Vt, const double *Ut, double *out) {
+  return guarded([&] {
+    check_dims(dims);
+    if (dims->Lx != dims->Ly || dims->Lx != dims->Lz)
+      throw std::runtime_error("displaced operators need a cubic lattice");
+    long const dim_row = 3L * dims->Lx * dims->Ly * dims->Lz;
+    std::vector<int> iup, idown;
+    gauge_neighbours(dims->Lx, dims->Ly, iup, idown);
+    Mat res(static_cast<int>(dim_row), dims->nev);
+    cd const *V = reinterpret_cast<cd const *>(Vt);
+    std::copy(V, V + dim_row * dims->nev, res.d.begin());
+    displace(res, reinterpret_cast<cd const *>(Ut), *op, iup, idown);
+    std::copy(res.d.begin(), res.d.end(), reinterpret_cast<cd *>(out));
   });
 }
 

@@ -66,6 +66,18 @@ int oracle_vdaggerv_gauge(const slaph_dims *dims, const slaph_vdv_op *ops, int n
 int oracle_vdaggerv_columns_dd(const slaph_dims *dims, const int p[3], const double *Vt,
                                const int *cols, int n_cols, double *out);
 
+/* The same for V_t^H W with W given (e.g. displaced eigenvectors from
+ * oracle_displace_eigenvectors), W: 2*3L^3*nev doubles column-major. */
+int oracle_vdaggerv_columns_dd_w(const slaph_dims *dims, const double *Vt, const double *Wt,
+                                 const int *cols, int n_cols, double *out);
+
+/* D(V_t) of one displaced operator (displace_eigenvectors,
+ * src/OperatorFactory.cpp:33-55, in the reference's in-place sweep order) on
+ * the timeslice's links Ut ([site][dir x,y,z][3x3 column-major]).
+ * out: 2*3L^3*nev doubles column-major. */
+int oracle_displace_eigenvectors(const slaph_dims *dims, const slaph_vdv_op *op,
+                                 const double *Vt, const double *Ut, double *out);
+
 /* GaugeField::smearing_hyp (src/GaugeField.cpp:322-427) of every timeslice,
  * in place on U[t] (layout as above), with proj_to_su3_imp (:203-210) taking
  * (M^H M)^(-1/2) from a Jacobi eigen-decomposition. */

@@ -63,6 +63,10 @@ int slaph_engine_set_random_vector_async(slaph_engine *eng, int32_t rnd_id,
   return slaph::guarded([&] { get(eng).set_random_vector(rnd_id, noise, true); });
 }
 
+int slaph_engine_set_eigenvector_slots(slaph_engine *eng, int32_t n_slots) {
+  return slaph::guarded([&] { get(eng).set_eigenvector_slots(n_slots); });
+}
+
 int slaph_engine_set_time_dilution(slaph_engine *eng, int32_t dilT) {
   return slaph::guarded([&] { get(eng).set_time_dilution(dilT); });
 }
@@ -161,7 +165,7 @@ int slaph_engine_timings(const slaph_engine *eng, double *out, int n) {
     slaph::set_last_error("invalid argument");
     return -1;
   }
-  int const m = n < 13 ? n : 13;
+  int const m = n < 14 ? n : 14;
   for (int i = 0; i < m; ++i) out[i] = eng->e->timings[i];
   return m;
 }

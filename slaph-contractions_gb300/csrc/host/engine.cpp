@@ -105,7 +105,9 @@ Engine::Engine(slaph_dims const &d) : dims_(d) {
   SLAPH_CK(cudaEventCreateWithFlags(&ev_pn_used_, cudaEventDisableTiming));
   SLAPH_CK(cudaEventRecord(ev_v_used_, stream_));
   SLAPH_CK(cudaEventRecord(ev_pn_used_, stream_));
-  V_.reserve(sizeof(double2) * geo_.dim_row * d.nev * d.Lt);
+  for (auto &e : ev_half_) SLAPH_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  // The eigenvectors are allocated by the first set_eigenvectors (all
+  // timeslices) or by set_eigenvector_slots (a ring).
   peram_.reserve(sizeof(double2) * peram_elems() * d.n_rnd);
   noise_.reserve(sizeof(double2) * 4LL * d.nev * d.Lt * d.n_rnd);
   SLAPH_CK(cudaMemsetAsync(noise_.as<void>(), 0, noise_.size(), stream_));
@@ -124,6 +126,8 @@ Engine::~Engine() {
     for (auto &e : *v)
       if (e) cudaEventDestroy(e);
   if (ev_v_used_) cudaEventDestroy(ev_v_used_);
+  for (auto &e : ev_half_)
+    if (e) cudaEventDestroy(e);
   if (ev_pn_used_) cudaEventDestroy(ev_pn_used_);
   if (up_stream_) cudaStreamDestroy(up_stream_);
   for (auto *v : {&tc_ev_, &vdv_ev_})
@@ -170,9 +174,30 @@ void Engine::set_operators(slaph_vdv_op const *ops, int32_t n, int32_t index_of_
   vdv_built_ = false;
 }
 
+void Engine::set_eigenvector_slots(int32_t n) {
+  if (n < 0 || n == 1) throw ArgError("eigenvector slots: 0 (all resident) or at least 2");
+  SLAPH_CK(cudaStreamSynchronize(up_stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  ring_slots_ = n;
+  V_.release();
+  std::fill(pend_v_.begin(), pend_v_.end(), 0);
+  host_v_.assign(dims_.Lt, nullptr);
+  if (n > 0) V_.reserve(sizeof(double2) * geo_.dim_row * dims_.nev * n);
+  vdv_built_ = false;
+}
+
 void Engine::set_eigenvectors(int32_t t, double const *V, bool async) {
   if (t < 0 || t >= dims_.Lt || !V) throw ArgError("invalid timeslice or null pointer");
   size_t const n = static_cast<size_t>(geo_.dim_row) * dims_.nev;
+  if (ring_slots_ > 0) {
+    // Streamed: the build copies timeslice t from this buffer when it needs it.
+    host_v_[t] = V;
+    return;
+  }
+  if (V_.size() < sizeof(double2) * n * dims_.Lt) {
+    SLAPH_CK(cudaStreamSynchronize(stream_));
+    V_.reserve(sizeof(double2) * n * dims_.Lt);
+  }
   // The previous VdaggerV build must be done with V before it is overwritten.
   SLAPH_CK(cudaStreamWaitEvent(up_stream_, ev_v_used_, 0));
   SLAPH_CK(cudaMemcpyAsync(V_.as<double2>() + n * t, V, n * sizeof(double2),
@@ -255,11 +280,14 @@ void Engine::smear_gauge_hyp(double alpha1, double alpha2, int32_t iterations) {
   hyp_dec_.reserve(per_dec * chunk);
   size_t const per = static_cast<size_t>(geo_.dim_row / 3) * 27;
   SLAPH_CK(cudaStreamWaitEvent(stream_, ev_v_used_, 0));
+  SLAPH_CK(cudaEventRecord(ev_[6], stream_));
   for (int32_t it = 0; it < iterations; ++it)
     for (int32_t t0 = 0; t0 < dims_.Lt; t0 += chunk)
       SLAPH_CK(dev::hyp_smear(U_.as<double2>() + per * t0, hyp_dec_.as<double2>(), dims_.Lx,
                               std::min(chunk, dims_.Lt - t0), alpha1, alpha2, stream_));
+  SLAPH_CK(cudaEventRecord(ev_[7], stream_));
   SLAPH_CK(cudaStreamSynchronize(stream_));
+  timings[13] = elapsed_ms(ev_[6], ev_[7]);
 }
 
 void Engine::gauge_fetch(int32_t t, double *out) {
@@ -322,7 +350,8 @@ void Engine::vdaggerv_build(int precision) {
                            U_.as<double2>(), W_.as<double2>(), phase_unit_.as<longlong2>(),
                            unit_op_.as<int32_t>()};
   }
-  int32_t n_gemm = 0;
+  int32_t n_gemm = 0;     // GEMM launches of the whole build
+  int64_t batch_fit = 1;  // timeslices per GEMM launch that the scratch holds
   if (precision == SLAPH_MIXED) {
     int sms = 0;
     SLAPH_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
@@ -330,75 +359,116 @@ void Engine::vdaggerv_build(int precision) {
     tc_scratch_.reserve(dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), batch));
     // The scratch may be larger than this batch needs (kept from an earlier
     // call): the launch count follows from what it holds.
-    int64_t const fits = static_cast<int64_t>(
-        tc_scratch_.size() / dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), 1));
-    n_gemm = n_all > 0 ? dev::vdaggerv_tc_gemm_launches(
-                             dims_.Lt, static_cast<int32_t>(std::max<int64_t>(1, fits)))
-                       : 0;
-    while (vdv_ev_.size() < 2 * static_cast<size_t>(n_gemm)) {
-      cudaEvent_t e = nullptr;
-      SLAPH_CK(cudaEventCreate(&e));
-      vdv_ev_.push_back(e);
-    }
+    batch_fit = std::max<int64_t>(
+        1, static_cast<int64_t>(tc_scratch_.size() /
+                                dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), 1)));
     err_.reserve(sizeof(int));
     SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
   }
+  // Timeslice ranges: all of them at once with resident eigenvectors, chunks
+  // of half the ring when they are streamed (one half is copied while the
+  // other is computed).
+  int32_t const chunk = ring_slots_ > 0 ? ring_slots_ / 2 : dims_.Lt;
+  std::vector<std::pair<int32_t, int32_t>> ranges;
+  for (int32_t t0 = 0; t0 < dims_.Lt; t0 += chunk)
+    ranges.emplace_back(t0, std::min(chunk, dims_.Lt - t0));
+  if (precision == SLAPH_MIXED && n_all > 0)
+    for (auto const &r : ranges)
+      n_gemm += dev::vdaggerv_tc_gemm_launches(r.second, static_cast<int32_t>(batch_fit));
+  while (vdv_ev_.size() < 2 * static_cast<size_t>(n_gemm)) {
+    cudaEvent_t e = nullptr;
+    SLAPH_CK(cudaEventCreate(&e));
+    vdv_ev_.push_back(e);
+  }
+  bool const needs_v = n_all > 0 || !displaced.empty();
+  if (ring_slots_ > 0 && needs_v)
+    for (int32_t t = 0; t < dims_.Lt; ++t)
+      if (!host_v_[t])
+        throw StateError("streamed eigenvectors: slaph_engine_set_eigenvectors is needed for "
+                         "every timeslice before the build");
+  if (ring_slots_ == 0 && needs_v && V_.size() == 0)
+    throw StateError("slaph_engine_set_eigenvectors must be called before the build");
   SLAPH_CK(cudaEventRecord(ev_[0], stream_));
   // Eigenvectors uploaded asynchronously: the split-precision build waits for
   // each timeslice just before slicing it (overlapping the remaining copies),
-  // the FP64 build for all of them.
+  // the FP64 build for the timeslices of its range.
   std::vector<cudaEvent_t> ready(dims_.Lt, nullptr);
-  for (int32_t t = 0; t < dims_.Lt; ++t)
-    if (pend_v_[t]) ready[t] = ev_v_[t];
-  if (precision == SLAPH_MIXED) {
-    launch(dev::vdaggerv_tc(vdv_.as<double2>(), V_.as<double2>(), phase_fx_.as<longlong2>(),
-                            list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_,
-                            tc_scratch_.as<void>(), tc_scratch_.size(), err_.as<int>(), stream_,
-                            ready.data(), tc_disp ? &dd : nullptr, vdv_ev_.data(),
-                            2 * n_gemm),
-           "vdaggerv_tc");
-    // per timeslice three slicing kernels, and per displaced operator its
-    // steps, exponents and slicing; one GEMM per timeslice batch
-    int64_t const per = static_cast<int64_t>(
-        tc_scratch_.size() / dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), 1));
-    int64_t disp_launches = 0;
-    for (int32_t n : d_n) disp_launches += n + 2;
-    launches_ += (3LL + disp_launches) * dims_.Lt +
-                 (dims_.Lt + per - 1) / std::max<int64_t>(per, 1) - 1 - (n_comp > 0 ? 0 : dims_.Lt);
-  } else {
-    for (auto e : ready)
-      if (e) SLAPH_CK(cudaStreamWaitEvent(stream_, e, 0));
-    launch(dev::vdaggerv_fp64(vdv_.as<double2>(), V_.as<double2>(), phase_.as<double2>(),
-                              list.as<int32_t>(), n_comp, 0, dims_.Lt, geo_, stream_),
-           "vdaggerv_fp64");
-  }
-  // Displaced operators of the FP64 build: W = D(V_t) step by step, then
-  // V_t^H W in FP64 (src/OperatorFactory.cpp:289-290, 300); the momentum is
-  // not applied.
-  if (!displaced.empty() && !tc_disp) {
-    for (auto e : ready)
-      if (e) SLAPH_CK(cudaStreamWaitEvent(stream_, e, 0));
-    size_t const n = static_cast<size_t>(geo_.dim_row) * dims_.nev;
-    size_t const per = static_cast<size_t>(geo_.dim_row / 3) * 27;
-    W_.reserve(sizeof(double2) * n);
+  if (ring_slots_ == 0)
+    for (int32_t t = 0; t < dims_.Lt; ++t)
+      if (pend_v_[t]) ready[t] = ev_v_[t];
+  size_t const n_v = static_cast<size_t>(geo_.dim_row) * dims_.nev;  // per timeslice
+  size_t const links = static_cast<size_t>(geo_.dim_row / 3) * 27;
+  bool const fp64_disp = !displaced.empty() && !tc_disp;
+  if (fp64_disp) {
+    W_.reserve(sizeof(double2) * n_v);
     upload(disp_ops_, displaced, stream_);
-    for (size_t k = 0; k < displaced.size(); ++k) {
-      slaph_vdv_op const &op = ops_[displaced[k]];
-      for (int32_t t = 0; t < dims_.Lt; ++t) {
-        SLAPH_CK(cudaMemcpyAsync(W_.as<double2>(), V_.as<double2>() + n * t, n * sizeof(double2),
-                                 cudaMemcpyDeviceToDevice, stream_));
-        for (int32_t s = 0; s < op.n_disp; ++s) {
-          char const ax = op.disp[2 * s + 1];
-          launch(dev::displace(W_.as<double2>(), U_.as<double2>() + per * t,
-                               ax == 'x' ? 0 : ax == 'y' ? 1 : 2, op.disp[2 * s] == '>' ? 1 : 0,
-                               geo_, stream_),
-                 "displace");
+  }
+  int64_t disp_launches = 0;  // per timeslice, split-precision displaced operators
+  for (int32_t n : d_n) disp_launches += n + 2;
+  int32_t gemm_done = 0;
+  for (size_t c = 0; c < ranges.size(); ++c) {
+    int32_t const t0 = ranges[c].first, nt = ranges[c].second;
+    double2 *Vb = V_.as<double2>();  // consecutive timeslices from v_t0 on
+    int32_t v_t0 = 0;
+    if (ring_slots_ > 0) {
+      int const h = static_cast<int>(c % 2);
+      Vb = V_.as<double2>() + n_v * static_cast<size_t>(chunk) * h;
+      v_t0 = t0;
+      if (needs_v) {
+        // This half was last read by the range two before this one.
+        if (c >= 2) SLAPH_CK(cudaStreamWaitEvent(up_stream_, ev_half_[h], 0));
+        for (int32_t t = t0; t < t0 + nt; ++t) {
+          SLAPH_CK(cudaMemcpyAsync(Vb + n_v * (t - t0), host_v_[t], n_v * sizeof(double2),
+                                   cudaMemcpyHostToDevice, up_stream_));
+          SLAPH_CK(cudaEventRecord(ev_v_[t], up_stream_));
+          ready[t] = ev_v_[t];
         }
-        launch(dev::vdaggerv_fp64_w(vdv_.as<double2>(), V_.as<double2>(), W_.as<double2>(),
-                                    disp_ops_.as<int32_t>() + k, t, geo_, stream_),
-               "vdaggerv_fp64_w");
       }
     }
+    if (precision == SLAPH_MIXED) {
+      int32_t const k =
+          n_all > 0 ? dev::vdaggerv_tc_gemm_launches(nt, static_cast<int32_t>(batch_fit)) : 0;
+      launch(dev::vdaggerv_tc(vdv_.as<double2>(), Vb, phase_fx_.as<longlong2>(),
+                              list.as<int32_t>(), n_comp, t0, nt, geo_, tc_scratch_.as<void>(),
+                              tc_scratch_.size(), err_.as<int>(), stream_, ready.data(),
+                              tc_disp ? &dd : nullptr, vdv_ev_.data() + 2 * gemm_done, 2 * k,
+                              v_t0, c == 0),
+             "vdaggerv_tc");
+      gemm_done += k;
+      // per timeslice the exponents, A slices and (with momentum operators)
+      // B slices, per displaced operator its steps, exponents and slices; one
+      // GEMM per batch of timeslices
+      if (n_all > 0)
+        launches_ += (2LL + (n_comp > 0 ? 1 : 0) + disp_launches) * nt + k - 1;
+    } else {
+      for (int32_t t = t0; t < t0 + nt; ++t)
+        if (ready[t]) SLAPH_CK(cudaStreamWaitEvent(stream_, ready[t], 0));
+      launch(dev::vdaggerv_fp64(vdv_.as<double2>(), Vb, phase_.as<double2>(), list.as<int32_t>(),
+                                n_comp, t0, nt, geo_, stream_, v_t0),
+             "vdaggerv_fp64");
+    }
+    // Displaced operators of the FP64 build: W = D(V_t) step by step, then
+    // V_t^H W in FP64 (src/OperatorFactory.cpp:289-290, 300); the momentum is
+    // not applied.
+    if (fp64_disp) {
+      for (int32_t t = t0; t < t0 + nt; ++t)
+        for (size_t k = 0; k < displaced.size(); ++k) {
+          slaph_vdv_op const &op = ops_[displaced[k]];
+          SLAPH_CK(cudaMemcpyAsync(W_.as<double2>(), Vb + n_v * (t - v_t0),
+                                   n_v * sizeof(double2), cudaMemcpyDeviceToDevice, stream_));
+          for (int32_t st = 0; st < op.n_disp; ++st) {
+            char const ax = op.disp[2 * st + 1];
+            launch(dev::displace(W_.as<double2>(), U_.as<double2>() + links * t,
+                                 ax == 'x' ? 0 : ax == 'y' ? 1 : 2,
+                                 op.disp[2 * st] == '>' ? 1 : 0, geo_, stream_),
+                   "displace");
+          }
+          launch(dev::vdaggerv_fp64_w(vdv_.as<double2>(), Vb, W_.as<double2>(),
+                                      disp_ops_.as<int32_t>() + k, t, geo_, stream_, v_t0),
+                 "vdaggerv_fp64_w");
+        }
+    }
+    if (ring_slots_ > 0) SLAPH_CK(cudaEventRecord(ev_half_[c % 2], stream_));
   }
   // V is not read after this point: later uploads may overwrite it.
   SLAPH_CK(cudaEventRecord(ev_v_used_, stream_));

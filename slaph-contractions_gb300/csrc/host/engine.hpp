@@ -91,6 +91,10 @@ class Engine {
   // for displaced operators.
   void set_gauge(int32_t t, double const *U);
   void set_time_dilution(int32_t dilT);
+  // 0: every eigenvector timeslice resident on the device (the default);
+  // n >= 2: a ring of n timeslice slots, filled from the host buffers given to
+  // set_eigenvectors during vdaggerv_build, n / 2 timeslices at a time.
+  void set_eigenvector_slots(int32_t n);
   // HYP smearing of the stored links of every timeslice, in place.
   void smear_gauge_hyp(double alpha1, double alpha2, int32_t iterations);
   void gauge_fetch(int32_t t, double *out);
@@ -126,6 +130,11 @@ class Engine {
   DevBuf hyp_dec_;           // decorated links of a chunk of timeslices (HYP smearing)
   DevBuf phase_unit_, unit_op_;  // phase 1 per site and its operator index (displaced, mixed)
   std::vector<char> gauge_set_;
+  // Eigenvector ring (set_eigenvector_slots): host buffer per timeslice and
+  // the compute stream's last use of each half of the ring.
+  int32_t ring_slots_ = 0;
+  std::vector<double const *> host_v_;
+  cudaEvent_t ev_half_[2] = {};
   int32_t index_of_unity_ = -1;
   bool ops_set_ = false, vdv_built_ = false;
   int64_t launches_ = 0;

@@ -73,18 +73,20 @@ cudaError_t displace(double2 *W, double2 const *U, int32_t dir, int32_t forward,
                      cudaStream_t stream);
 // VdaggerV[2 op][t] = V_t^H W in FP64 (*op: device pointer to the operator id).
 cudaError_t vdaggerv_fp64_w(double2 *vdv, double2 const *V, double2 const *W,
-                            int32_t const *op, int32_t t, Geometry g, cudaStream_t stream);
+                            int32_t const *op, int32_t t, Geometry g, cudaStream_t stream,
+                            int32_t v_t0 = 0);
 // exp(-i p.x) for every op: phase[op][x] (create_momenta,
 // src/OperatorFactory.cpp:64-95).  mom: [n_ops][3].
 cudaError_t momenta(double2 *phase, int32_t const *mom, int32_t n_ops, Geometry g,
                     cudaStream_t stream);
 
 // VdaggerV[vdv code 2*op][t] = V_t^H diag(phase[op] per site) V_t for every op
-// in ops[0..n) (src/OperatorFactory.cpp:292-300), FP64.  V: [Lt][nev][dim_row]
-// (each timeslice column-major).  vdv: [2*n_ops][Lt][nev][nev].
+// in ops[0..n) (src/OperatorFactory.cpp:292-300), FP64.  V: consecutive
+// timeslices [t][nev][dim_row] (each column-major), V[0] holding timeslice
+// v_t0 (0: all Lt resident; a ring slot otherwise).  vdv: [2*n_ops][Lt][nev][nev].
 cudaError_t vdaggerv_fp64(double2 *vdv, double2 const *V, double2 const *phase,
                           int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
-                          cudaStream_t stream);
+                          cudaStream_t stream, int32_t v_t0 = 0);
 // Split-BF16 tensor-core VdaggerV (vdv_tc.cu): same result as vdaggerv_fp64
 // to ~1e-13 relative.  scratch: device buffer of at least
 // vdaggerv_tc_scratch_bytes(g, n, batch) bytes, where batch timeslices are
@@ -116,9 +118,13 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
                         cudaEvent_t const *t_ready = nullptr,
                         VdvDisplaced const *disp = nullptr,
-                        cudaEvent_t const *gemm_ev = nullptr, int32_t n_gemm_ev = 0);
-// (t_ready[t], when given and non-null: event after which timeslice t of V is
-// valid; the slicing of t waits for it on `stream`.  gemm_ev: when given, the
+                        cudaEvent_t const *gemm_ev = nullptr, int32_t n_gemm_ev = 0,
+                        int32_t v_t0 = 0, bool clear_scratch = true);
+// (V: consecutive timeslices, V[0] holding timeslice v_t0.  clear_scratch:
+// zero the scratch slots first (their padding rows must be zero); a later
+// call on the same scratch in the same build may skip it.  t_ready[t], when
+// given and non-null: event after which timeslice t of V is valid; the
+// slicing of t waits for it on `stream`.  gemm_ev: when given, the
 // events 2k and 2k+1 are recorded on `stream` just before and after the k-th
 // GEMM launch, for k < n_gemm_ev / 2; vdaggerv_tc_gemm_launches gives k's range.)
 int32_t vdaggerv_tc_gemm_launches(int32_t nt, int32_t batch);

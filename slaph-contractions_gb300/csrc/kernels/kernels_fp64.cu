@@ -94,7 +94,8 @@ template <bool kW>
 __global__ void __launch_bounds__(256) vdv_fp64_kernel(double2 *vdv, double2 const *V,
                                                        double2 const *phase,
                                                        int32_t const *ops, int32_t t0,
-                                                       Geometry g, double2 const *W) {
+                                                       Geometry g, double2 const *W,
+                                                       int32_t v_t0) {
   __shared__ double2 As[VK][VT];
   __shared__ double2 Bs[VK][VT];
   int const nev = g.nev;
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(256) vdv_fp64_kernel(double2 *vdv, double2 con
   int const op = ops[blockIdx.y];
   int const t = t0 + blockIdx.z;
   int const tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-  double2 const *Vt = V + static_cast<int64_t>(t) * nev * dim_row;
+  double2 const *Vt = V + static_cast<int64_t>(t - v_t0) * nev * dim_row;
   double2 const *ph = kW ? nullptr : phase + static_cast<int64_t>(op) * vol;
   double2 acc[4][4];
 #pragma unroll
@@ -583,11 +584,11 @@ cudaError_t momenta(double2 *phase, int32_t const *mom, int32_t n_ops, Geometry 
 
 cudaError_t vdaggerv_fp64(double2 *vdv, double2 const *V, double2 const *phase,
                           int32_t const *ops, int32_t n, int32_t t0, int32_t nt, Geometry g,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, int32_t v_t0) {
   if (n == 0 || nt == 0) return cudaSuccess;
   int const tiles = (g.nev + VT - 1) / VT;
   dim3 grid(tiles * tiles, n, nt);
-  vdv_fp64_kernel<false><<<grid, 256, 0, stream>>>(vdv, V, phase, ops, t0, g, nullptr);
+  vdv_fp64_kernel<false><<<grid, 256, 0, stream>>>(vdv, V, phase, ops, t0, g, nullptr, v_t0);
   return cudaGetLastError();
 }
 
@@ -670,10 +671,11 @@ cudaError_t displace(double2 *W, double2 const *U, int32_t dir, int32_t forward,
 }
 
 cudaError_t vdaggerv_fp64_w(double2 *vdv, double2 const *V, double2 const *W,
-                            int32_t const *op, int32_t t, Geometry g, cudaStream_t stream) {
+                            int32_t const *op, int32_t t, Geometry g, cudaStream_t stream,
+                            int32_t v_t0) {
   int const tiles = (g.nev + VT - 1) / VT;
   vdv_fp64_kernel<true><<<dim3(tiles * tiles, 1, 1), 256, 0, stream>>>(vdv, V, nullptr, op, t,
-                                                                       g, W);
+                                                                       g, W, v_t0);
   return cudaGetLastError();
 }
 

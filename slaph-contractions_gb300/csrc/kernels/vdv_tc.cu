@@ -8,8 +8,10 @@
 //
 // Data path: slices are written once per timeslice (A) and per timeslice and
 // operator (B) to HBM, already in the tcgen05 core-matrix layout, and streamed
-// into shared memory by the GEMM (grid: m tiles x n tiles x operators x
-// timeslices of a batch).
+// into shared memory by the GEMM.  The B columns of all operators of a
+// timeslice form one N dimension (column o nev + j: operator o, eigenvector
+// j), cut into tiles of kTN without padding between operators; grid: m tiles x
+// n tiles x timeslices of a batch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -61,46 +63,45 @@ __global__ void slice_a_kernel(uint16_t *out, double2 const *Vt, int32_t const *
   put_a(reinterpret_cast<uint8_t *>(out), k_tiles, i, x, v, expo[i]);
 }
 
-// B slices of W = diag(phase_op) V for all operators of the call:
-// [op][n_tile][k_tile][slice][kTN x kTK].  A warp covers one 8-column row
-// group of one k-tile: lane (r, kg) = (lane % 8, lane / 8) takes column
-// 8 rg + r and the 4 complex K entries 4 kg .. 4 kg + 3, i.e. one 16-byte row of
-// core matrix (rg, kg), so that each slice store of the warp writes 512
-// contiguous bytes.  V is read and put in fixed point once for all operators;
-// the phase product is taken in fixed point with integer operations only: with
-// V = F_v 2^(e-55) and phase = P 2^-62 (|P| <= 2^62),
-// W = ((F_v 4) P / 2^64) 2^(e-55), the high word of a 128-bit product.
-// Padding columns (j >= nev) and K entries (x >= dim_row) are written as zero.
+// B slices of W = diag(phase_op) V for the operators ops[0..n_ops) of the
+// call, at global B columns col0 + o nev + j: [n_tile][k_tile][slice][kTN x kTK]
+// over the columns of all operators.  A warp covers one 8-column group of one
+// operator's eigenvectors in one k-tile: lane (r, kg) = (lane % 8, lane / 8)
+// takes eigenvector 8 rg + r and the 4 complex K entries 4 kg .. 4 kg + 3, i.e.
+// one 16-byte row of a core matrix, so that the slice stores of the warp cover
+// one or two 8-row core-matrix columns.  V is read and put in fixed point once
+// for all operators; the phase product is taken in fixed point with integer
+// operations only: with V = F_v 2^(e-55) and phase = P 2^-62 (|P| <= 2^62),
+// W = ((F_v 4) P / 2^64) 2^(e-55), the high word of a 128-bit product.  K
+// entries x >= dim_row are written as zero; columns past the last operator's
+// stay as the per-build clear of the scratch left them (zero).
 __global__ void __launch_bounds__(256)
     slice_b_kernel(uint8_t *out, double2 const *Vt, longlong2 const *phase_fx,
                    int32_t const *ops, int32_t n_ops, int32_t const *expo, int32_t k_tiles,
-                   int32_t n_tiles, Geometry g) {
+                   int64_t col0, Geometry g) {
   int64_t const wid = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / 32;
   int const lane = threadIdx.x % 32;
-  int64_t const groups = static_cast<int64_t>(n_tiles) * (kTN / 8);
+  int64_t const groups = (g.nev + 7) / 8;
   if (wid >= groups * k_tiles) return;
   int64_t const kt = wid / groups;
-  int const rgg = static_cast<int>(wid % groups);  // row group over all n tiles
-  int const nt = rgg / (kTN / 8), rg = rgg % (kTN / 8);
+  int const rg = static_cast<int>(wid % groups);
   int const r = lane % 8, kg = lane / 8;
-  int const j = rgg * 8 + r;
+  int const j = rg * 8 + r;
+  if (j >= g.nev) return;
   int64_t const x0 = kt * (kTK / 2) + 4 * kg;
   int64_t const sites = g.dim_row / 3;
   long long vr[4], vi[4];
   int64_t site[4];
-  int const e = j < g.nev ? expo[j] : 0;
+  int const e = expo[j];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     int64_t const x = x0 + q;
-    bool const in = j < g.nev && x < g.dim_row;
+    bool const in = x < g.dim_row;
     double2 const v = in ? Vt[static_cast<int64_t>(j) * g.dim_row + x] : make_double2(0, 0);
     vr[q] = fixed55(v.x, e) * 4;
     vi[q] = fixed55(v.y, e) * 4;
     site[q] = in ? x / 3 : 0;
   }
-  uint8_t *dst0 = out + (static_cast<int64_t>(nt) * k_tiles + kt) * kStageB +
-                  (rg * 4 + kg) * 128 + r * 16;
-  int64_t const op_stride = static_cast<int64_t>(n_tiles) * k_tiles * kStageB;
   for (int o = 0; o < n_ops; ++o) {
     longlong2 const *ph = phase_fx + static_cast<int64_t>(ops[o]) * sites;
     uint32_t w[kSlices][4];
@@ -115,7 +116,10 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int s = 0; s < kSlices; ++s) w[s][q] = bf16x2(dre[s], dim[s]);
     }
-    uint8_t *dst = dst0 + o * op_stride;
+    int64_t const gc = col0 + static_cast<int64_t>(o) * g.nev + j;
+    int64_t const nt = gc / kTN;
+    int const rr = static_cast<int>(gc % kTN);
+    uint8_t *dst = out + (nt * k_tiles + kt) * kStageB + ((rr >> 3) * 4 + kg) * 128 + (rr & 7) * 16;
 #pragma unroll
     for (int s = 0; s < kSlices; ++s)
       *reinterpret_cast<uint4 *>(dst + s * kBBlk) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
@@ -129,14 +133,16 @@ __global__ void phase_fixed_kernel(longlong2 *dst, double2 const *src, int64_t n
   dst[k] = make_longlong2(__double2ll_rn(ldexp(v.x, 62)), __double2ll_rn(ldexp(v.y, 62)));
 }
 
-// Epilogue of one VdaggerV tile: D = (hi + lo) 2^(e_i + f_j - 14), rows
-// (2i, 2i+1) = (Re, Im) of VdaggerV(i, j), column-major nev x nev blocks; e:
-// exponents of the eigenvectors (A rows), f: those of the B columns (the same
-// for momentum operators, |phase| = 1; those of D(V) for displaced ones).
+// Epilogue of one VdaggerV tile: D = (hi + lo) 2^(e_i + f_c - 14), rows
+// (2i, 2i+1) = (Re, Im) of VdaggerV_o(i, j) for the tile's B columns c = o nev
+// + j, written to operator o's column-major nev x nev block of timeslice t; e:
+// exponents of the eigenvectors (A rows), f: those of the B columns (the
+// eigenvectors' for momentum operators, |phase| = 1; those of D(V) for the
+// displaced ones, o >= n_comp, at (1 + o) nev).
 struct VdvEpilogue {
-  double *outd;
-  int32_t const *expo, *expo_col;
-  int i0, j0, nev;
+  double2 *vdv;
+  int32_t const *expo, *ops;
+  int i0, c0, nev, n_comp, n_cols, Lt, t;
   __device__ __forceinline__ void operator()(int row, float const (&hi)[kTN],
                                              float const (&lo)[kTN]) const {
     int const i = i0 + row / 2;
@@ -144,38 +150,38 @@ struct VdvEpilogue {
     int const ei = expo[i];
 #pragma unroll
     for (int jj = 0; jj < kTN; ++jj) {
-      int const j = j0 + jj;
-      if (j < nev) {
+      int const c = c0 + jj;
+      if (c < n_cols) {
+        int const o = c / nev, j = c - o * nev;
+        int const ec = o < n_comp ? expo[j] : expo[(1 + o) * nev + j];
+        double *outd = reinterpret_cast<double *>(
+            vdv + (static_cast<int64_t>(2 * ops[o]) * Lt + t) * nev * nev);
         double const val = ldexp(static_cast<double>(hi[jj]) + static_cast<double>(lo[jj]),
-                                 ei + expo_col[j] - 14);
+                                 ei + ec - 14);
         outd[2 * (i + static_cast<int64_t>(nev) * j) + (row & 1)] = val;
       }
     }
   }
 };
 
-// The GEMM: grid (m_tiles, n_tiles, n_ops * batch), kThreads threads.  Batch
-// slot b (timeslice t0 + b) has its own A slices, B slices and exponents at
-// stride slot_bytes in the scratch buffer: the eigenvectors' exponents, then
-// per operator o >= n_comp (displaced) the exponents of its B columns at
+// The GEMM: grid (m_tiles, n_tiles, batch), kThreads threads.  Batch slot b
+// (timeslice t0 + b) has its own A slices, B slices and exponents at stride
+// slot_bytes in the scratch buffer: the eigenvectors' exponents, then per
+// operator o >= n_comp (displaced) the exponents of its B columns at
 // (1 + o) nev.
 __global__ void __launch_bounds__(kThreads, 1)
     ozaki_gemm_kernel(uint8_t const *scratch, size_t slot_bytes, size_t b_off, size_t e_off,
                       double2 *vdv, int32_t const *ops, int32_t n_ops, int32_t n_comp,
-                      int32_t k_tiles, int32_t n_tiles, int32_t t0, Geometry g, int *err) {
+                      int32_t k_tiles, int32_t t0, Geometry g, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  int const mt = blockIdx.x, nt = blockIdx.y;
-  int const o = blockIdx.z % n_ops, slot = blockIdx.z / n_ops;
+  int const mt = blockIdx.x, nt = blockIdx.y, slot = blockIdx.z;
   int const t = t0 + slot;
   uint8_t const *sbase = scratch + slot * slot_bytes;
   uint8_t const *a_src = sbase + static_cast<int64_t>(mt) * k_tiles * kStageA;
-  uint8_t const *b_src =
-      sbase + b_off + (static_cast<int64_t>(o) * n_tiles + nt) * k_tiles * kStageB;
+  uint8_t const *b_src = sbase + b_off + static_cast<int64_t>(nt) * k_tiles * kStageB;
   int32_t const *expo = reinterpret_cast<int32_t const *>(sbase + e_off);
-  VdvEpilogue epi{reinterpret_cast<double *>(vdv + (static_cast<int64_t>(2 * ops[o]) * g.Lt + t) *
-                                                       g.nev * g.nev),
-                  expo, o < n_comp ? expo : expo + static_cast<int64_t>(1 + o) * g.nev,
-                  mt * (kTM / 2), nt * kTN, g.nev};
+  VdvEpilogue epi{vdv, expo, ops, mt * (kTM / 2), nt * kTN, g.nev, n_comp, n_ops * g.nev,
+                  g.Lt, t};
   ozaki_tile(smem, a_src, b_src, k_tiles, err, epi);
 }
 
@@ -190,9 +196,9 @@ TcLayout tc_layout(Geometry const &g, int32_t n_ops) {
   TcLayout L{};
   L.k_tiles = (g.dim_row + kTK / 2 - 1) / (kTK / 2);
   L.m_tiles = (2LL * g.nev + kTM - 1) / kTM;
-  L.n_tiles = (g.nev + kTN - 1) / kTN;
+  L.n_tiles = (static_cast<int64_t>(n_ops) * g.nev + kTN - 1) / kTN;  // all operators
   L.a_bytes = static_cast<size_t>(L.m_tiles * L.k_tiles) * kStageA;
-  L.b_bytes = static_cast<size_t>(n_ops) * L.n_tiles * L.k_tiles * kStageB;
+  L.b_bytes = static_cast<size_t>(L.n_tiles * L.k_tiles) * kStageB;
   L.e_off = L.a_bytes + L.b_bytes;
   // exponents: the eigenvectors', then room for one set per operator
   L.slot_bytes =
@@ -207,7 +213,7 @@ size_t vdaggerv_tc_scratch_bytes(Geometry g, int32_t n_ops, int32_t batch) {
 
 int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes) {
   TcLayout const L = tc_layout(g, n_ops);
-  int64_t const ctas = L.m_tiles * L.n_tiles * n_ops;
+  int64_t const ctas = L.m_tiles * L.n_tiles;
   int64_t want = (2LL * sm_count + ctas - 1) / ctas;  // at least two waves
   if (want > g.Lt) want = g.Lt;
   int64_t const fit = static_cast<int64_t>(max_bytes / L.slot_bytes);
@@ -227,7 +233,8 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
                         int32_t const *ops, int32_t n_comp, int32_t t0, int32_t nt, Geometry g,
                         void *scratch, size_t scratch_bytes, int *err, cudaStream_t stream,
                         cudaEvent_t const *t_ready, VdvDisplaced const *disp,
-                        cudaEvent_t const *gemm_ev, int32_t n_gemm_ev) {
+                        cudaEvent_t const *gemm_ev, int32_t n_gemm_ev, int32_t v_t0,
+                        bool clear_scratch) {
   int32_t const n_disp = disp ? disp->n : 0;
   int32_t const n = n_comp + n_disp;
   if (n == 0 || nt == 0) return cudaSuccess;
@@ -243,15 +250,18 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(kSmemBytes));
   if (e != cudaSuccess) return e;
-  // Padding rows of the last tiles stay zero: clear the slots once per call.
-  e = cudaMemsetAsync(base, 0, L.slot_bytes * static_cast<size_t>(std::min<int64_t>(batch, nt)),
-                      stream);
-  if (e != cudaSuccess) return e;
+  // Padding rows of the last tiles are never written by the slicing: clear
+  // the slots once per build.
+  if (clear_scratch) {
+    e = cudaMemsetAsync(base, 0,
+                        L.slot_bytes * static_cast<size_t>(std::min<int64_t>(batch, nt)), stream);
+    if (e != cudaSuccess) return e;
+  }
   int64_t const xs = L.k_tiles * (kTK / 2);
   unsigned const xb = static_cast<unsigned>((xs + 255) / 256);
-  // slice_b_kernel: one warp per (k-tile, 8-column row group)
-  unsigned const bb = static_cast<unsigned>((L.k_tiles * L.n_tiles * (kTN / 8) * 32 + 255) / 256);
-  size_t const b_op = static_cast<size_t>(L.n_tiles * L.k_tiles) * kStageB;
+  // slice_b_kernel: one warp per (k-tile, group of 8 eigenvectors)
+  unsigned const bb =
+      static_cast<unsigned>((L.k_tiles * ((g.nev + 7) / 8) * 32 + 255) / 256);
   size_t const links = static_cast<size_t>(g.dim_row / 3) * 27;  // of one timeslice
   int32_t gemm_k = 0;
   for (int32_t tb = t0; tb < t0 + nt; tb += static_cast<int32_t>(batch)) {
@@ -262,7 +272,7 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
         e = cudaStreamWaitEvent(stream, t_ready[t], 0);
         if (e != cudaSuccess) return e;
       }
-      double2 const *Vt = V + static_cast<int64_t>(t) * g.nev * g.dim_row;
+      double2 const *Vt = V + static_cast<int64_t>(t - v_t0) * g.nev * g.dim_row;
       uint8_t *slot = base + b * L.slot_bytes;
       int32_t *expo = reinterpret_cast<int32_t *>(slot + L.e_off);
       colmax_kernel<<<g.nev, 256, 0, stream>>>(expo, Vt, g);
@@ -270,8 +280,7 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
           reinterpret_cast<uint16_t *>(slot), Vt, expo, static_cast<int32_t>(L.k_tiles), g);
       if (n_comp > 0)
         slice_b_kernel<<<bb, 256, 0, stream>>>(slot + L.a_bytes, Vt, phase_fx, ops, n_comp, expo,
-                                                static_cast<int32_t>(L.k_tiles),
-                                                static_cast<int32_t>(L.n_tiles), g);
+                                                static_cast<int32_t>(L.k_tiles), 0, g);
       // Displaced operators: W = D(V_t) in the reference's in-place sweep
       // order, B = W with phase 1 and W's own column exponents.
       for (int32_t d = 0; d < n_disp; ++d) {
@@ -286,10 +295,10 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
         }
         int32_t *expo_w = expo + static_cast<int64_t>(1 + o) * g.nev;
         colmax_kernel<<<g.nev, 256, 0, stream>>>(expo_w, disp->W, g);
-        slice_b_kernel<<<bb, 256, 0, stream>>>(slot + L.a_bytes + o * b_op, disp->W,
-                                                disp->unit_phase, disp->unit_op, 1, expo_w,
+        slice_b_kernel<<<bb, 256, 0, stream>>>(slot + L.a_bytes, disp->W, disp->unit_phase,
+                                                disp->unit_op, 1, expo_w,
                                                 static_cast<int32_t>(L.k_tiles),
-                                                static_cast<int32_t>(L.n_tiles), g);
+                                                static_cast<int64_t>(o) * g.nev, g);
       }
     }
     bool const timed = gemm_ev && 2 * gemm_k + 1 < n_gemm_ev;
@@ -298,11 +307,11 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
       if (e != cudaSuccess) return e;
     }
     ozaki_gemm_kernel<<<dim3(static_cast<unsigned>(L.m_tiles),
-                             static_cast<unsigned>(L.n_tiles),
-                             static_cast<unsigned>(n * nb)),
-                        kThreads, kSmemBytes, stream>>>(
-        base, L.slot_bytes, L.a_bytes, L.e_off, vdv, ops, n, n_comp,
-        static_cast<int32_t>(L.k_tiles), static_cast<int32_t>(L.n_tiles), tb, g, err);
+                             static_cast<unsigned>(L.n_tiles), static_cast<unsigned>(nb)),
+                        kThreads, kSmemBytes, stream>>>(base, L.slot_bytes, L.a_bytes, L.e_off,
+                                                        vdv, ops, n, n_comp,
+                                                        static_cast<int32_t>(L.k_tiles), tb, g,
+                                                        err);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (timed) {

@@ -122,6 +122,7 @@ PROTOTYPES = {
                                            C.c_char_p, C.c_size_t]),
     "slaph_engine_set_gauge": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_engine_set_time_dilution": (C.c_int, [C.c_void_p, _i32]),
+    "slaph_engine_set_eigenvector_slots": (C.c_int, [C.c_void_p, _i32]),
     "slaph_engine_smear_gauge_hyp": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _i32]),
     "slaph_engine_gauge_fetch": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_selftest_bounded_wait": (C.c_int, [_i64, C.POINTER(_i32)]),

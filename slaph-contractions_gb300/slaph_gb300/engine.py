@@ -85,6 +85,8 @@ class Engine:
         fn = (L.lib().slaph_engine_set_eigenvectors_async if asynchronous
               else L.lib().slaph_engine_set_eigenvectors)
         L.check(fn(self._h, t, L.dptr(V)))
+        if getattr(self, "_ring", False):
+            self._keep[t] = V  # read by the next build
 
     def set_perambulator(self, r, P, asynchronous=False):
         P = _c128(P)
@@ -97,6 +99,15 @@ class Engine:
         fn = (L.lib().slaph_engine_set_random_vector_async if asynchronous
               else L.lib().slaph_engine_set_random_vector)
         L.check(fn(self._h, r, L.dptr(noise)))
+
+    def set_eigenvector_slots(self, n_slots):
+        """Stream the eigenvectors through a ring of n_slots timeslices (>= 2),
+        or keep all resident (0); see slaph_engine_set_eigenvector_slots.  In
+        ring mode set_eigenvectors only records the array, which must stay
+        alive and unchanged until vdaggerv_build returns."""
+        L.check(L.lib().slaph_engine_set_eigenvector_slots(self._h, int(n_slots)))
+        self._ring = int(n_slots) > 0
+        self._keep = {}
 
     def set_time_dilution(self, dilT):
         """Slices per time-dilution block for the following contractions
@@ -162,9 +173,10 @@ class Engine:
     def timings(self):
         """ms: VdaggerV, factors, products+traces, assembly, planning; launches;
         per-entry trace kernel (ms, launches); trace GEMM (ms, launches);
-        operand slicing of the trace GEMM (ms); VdaggerV GEMM (ms, launches)."""
-        out = np.zeros(13)
-        L.lib().slaph_engine_timings(self._h, L.dptr(out), 13)
+        operand slicing of the trace GEMM (ms); VdaggerV GEMM (ms, launches);
+        HYP smearing (ms)."""
+        out = np.zeros(14)
+        L.lib().slaph_engine_timings(self._h, L.dptr(out), 14)
         return out
 
     def stats(self):

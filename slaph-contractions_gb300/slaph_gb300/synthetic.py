@@ -50,6 +50,13 @@ class Workload:
     # Quark lines replacing the single default one (flavours with the same
     # dilution; n_rnd is then their total number of random vectors).
     quark_lines: tuple = ()
+    # > 0: timeslice t has the eigenvectors of timeslice t % v_period, so that
+    # a workload whose eigenvectors exceed host memory needs only v_period of
+    # them; every timeslice is still copied and computed.
+    v_period: int = 0
+    # > 0: the engine streams the eigenvectors through this many device slots
+    # (slaph_engine_set_eigenvector_slots) instead of keeping all resident.
+    eigenvector_slots: int = 0
 
     @property
     def dim_row(self):
@@ -80,6 +87,8 @@ class Workload:
 
     def eigenvectors(self, t):
         """Timeslice t as (nev, 3L^3) C-order, i.e. column-major V_t."""
+        if self.v_period > 0:
+            t %= self.v_period
         rng = self._rng(1, t)
         K = self.dim_row
         a = rng.standard_normal((self.nev, 2 * K)).view(np.complex128)  # (nev, K)
@@ -88,6 +97,23 @@ class Workload:
             return np.ascontiguousarray(q.T)
         a /= np.linalg.norm(a, axis=1, keepdims=True)
         return a
+
+    def gauge_links(self, t):
+        """Random SU(3) links of timeslice t in the layout Engine.set_gauge
+        takes: complex (L^3, 3, 9), site x L^2 + y L + z, directions x, y, z,
+        each 3x3 matrix column-major.  Rows u1, u2 orthonormalised from complex
+        Gaussians and u3 = conj(u1 x u2), which puts the matrix in SU(3)."""
+        if self.v_period > 0:
+            t %= self.v_period
+        rng = self._rng(4, t)
+        n = self.L ** 3 * 3
+        z = rng.standard_normal((n, 2, 3)) + 1j * rng.standard_normal((n, 2, 3))
+        u1 = z[:, 0] / np.linalg.norm(z[:, 0], axis=1, keepdims=True)
+        u2 = z[:, 1] - np.sum(np.conj(u1) * z[:, 1], axis=1, keepdims=True) * u1
+        u2 /= np.linalg.norm(u2, axis=1, keepdims=True)
+        u3 = np.conj(np.cross(u1, u2))
+        M = np.stack([u1, u2, u3], axis=1)  # M[a, b] = u_a[b]
+        return np.ascontiguousarray(M.transpose(0, 2, 1)).reshape(self.L ** 3, 3, 9)
 
     def perambulator(self, r):
         """[cols][rows] (column-major storage of the re-sorted matrix)."""
@@ -191,3 +217,51 @@ def grouped_pipi(name, nev, dilE, seed):
 
 CONFIGS["pipi_groups_e4"] = grouped_pipi("pipi_groups_e4", nev=16, dilE=4, seed=606)
 CONFIGS["pipi_groups_e8"] = grouped_pipi("pipi_groups_e8", nev=32, dilE=8, seed=707)
+
+
+# 48^3 x 96, Nev 220 (eigenvectors 112 GB, streamed per timeslice): the pipi
+# I=1 set of the 32^3 x 64 workload, the KK set of infiles/KK.in (an s quark
+# beside the u quark) and one-derivative displaced operators in all six
+# directions on HYP-smeared links; 6 random vectors per flavour, TB16 EI8 DF4.
+_KK_OPS = ["g4.d0.p0", "g5.d0.p0", "g5.d>x,<x,>y,<y,>z,<z.p0"]
+CONFIGS["cfg5_48x96"] = Workload(
+    "cfg5_48x96", Lt=96, L=48, nev=220, n_rnd=12, dilT=16, dilE=8,
+    operators=PION_RHO_OPERATORS + _KK_OPS,
+    correlators=(["C2c:Q0:Op9:Q0:Op9:P0,1,2,3,4"]
+                 + [f"C3c:Q0:Op9:Q0:Op{k}:Q0:Op9:P0,1,2,3,4" for k in range(9)]
+                 + ["C4cD:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1,2,3,4",
+                    "C4cB:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1,2,3,4",
+                    "C4cV:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1,2,3,4",
+                    "C2c:Q0:Op11:Q1:Op11", "C4cD:Q0:Op11:Q1:Op11:Q0:Op11:Q1:Op11",
+                    "C4cC:Q0:Op11:Q1:Op11:Q0:Op11:Q1:Op11",
+                    "C20:Q0:Op10:Q1:Op10", "C40D:Q0:Op10:Q1:Op10:Q0:Op10:Q1:Op10",
+                    "C40V:Q0:Op10:Q1:Op10:Q0:Op10:Q1:Op10",
+                    "C40C:Q0:Op10:Q1:Op10:Q0:Op10:Q1:Op10",
+                    "C40B:Q0:Op10:Q1:Op10:Q0:Op10:Q1:Op10",
+                    "C2c:Q0:Op12:Q0:Op12:P0"]),
+    quark_lines=("u:6:TB:16:EI:8:DF:4:synthetic", "s:6:TB:16:EI:8:DF:4:synthetic"),
+    extra={"alpha1": 0.62, "alpha2": 0.62, "iterations": 3},
+    seed=909, orthonormal=False, v_period=8, eigenvector_slots=2,
+    description="48^3x96 Nev=220: pipi I=1 + KK + displaced, streamed eigenvectors")
+
+
+# Uneven batch: six configurations of 24^3 x 48 and 32^3 x 64 with Nev from 64
+# to 220, 3-6 random vectors and time dilution 8 or 16, the pion/rho operators
+# with |p|^2 <= 1 (instances with 3 random vectors drop the four-point
+# diagrams, which need four distinct random indices).
+def uneven_instance(i, L, Lt, nev, n_rnd, dilT):
+    ops = [o.replace("p0,1,2,3,4", "p0,1") for o in PION_RHO_OPERATORS]
+    corr = (["C2c:Q0:Op9:Q0:Op9:P0,1"]
+            + [f"C3c:Q0:Op9:Q0:Op{k}:Q0:Op9:P0,1" for k in range(9)])
+    if n_rnd >= 4:
+        corr += ["C4cD:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1",
+                 "C4cB:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1",
+                 "C4cV:Q0:Op9:Q0:Op9:Q0:Op9:Q0:Op9:P0,1"]
+    return Workload(f"cfg4_{i}_{L}x{Lt}_nev{nev}", Lt=Lt, L=L, nev=nev, n_rnd=n_rnd, dilT=dilT,
+                    dilE=8, operators=ops, correlators=corr, seed=1000 + i, orthonormal=False,
+                    description=f"{L}^3x{Lt} Nev={nev}, {n_rnd} random vectors, TB{dilT}")
+
+
+UNEVEN_CFG4 = [uneven_instance(i, *a) for i, a in enumerate([
+    (24, 48, 64, 3, 8), (24, 48, 96, 4, 16), (24, 48, 120, 5, 8),
+    (32, 64, 160, 6, 16), (32, 64, 220, 4, 16), (32, 64, 120, 5, 8)])]

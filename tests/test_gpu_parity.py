@@ -816,3 +816,64 @@ def test_bounded_device_wait_gives_up_and_the_context_stays_usable(l4):
     names = [n for _, ds in l4["gd"].output_layout() for n in ds]
     assert max(float(np.max(np.abs(v - golden[n]))) for n, v in zip(names, out)) < 1e-10
     assert corr_rel_err(out, np.stack([golden[n] for n in names])) < REL_MIXED_CORR
+
+
+# ---------------------------------------------------------------- streamed eigenvectors
+@pytest.mark.parametrize("slots", [2, 6])
+def test_streamed_eigenvectors_match_resident(tmp_path, slots):
+    """slaph_engine_set_eigenvector_slots: eigenvectors copied into a ring of
+    `slots` timeslices during the build (the reference reads them per
+    timeslice inside its VdaggerV loop, src/OperatorFactory.cpp:263-300) give
+    exactly the VdaggerV blocks and correlators of resident eigenvectors, in
+    both precisions, with momentum and displaced operators, for chunks that do
+    and do not divide Lt (8 timeslices in chunks of 1 and 3)."""
+    from slaph_gb300 import GlobalData, synthetic
+    from slaph_gb300.engine import Engine
+    ops = ["g5.d0.p0,1", "g1.d0.p0,1", "g5.d>x.p0"]
+    w = synthetic.Workload("stream", Lt=8, L=4, nev=16, n_rnd=4, dilT=2, dilE=4,
+                           operators=ops,
+                           correlators=["C2c:Q0:Op0:Q0:Op0:P0,1", "C3c:Q0:Op0:Q0:Op1:Q0:Op0:P0,1",
+                                        "C2c:Q0:Op2:Q0:Op2:P0",
+                                        "C4cD:Q0:Op0:Q0:Op0:Q0:Op0:Q0:Op0:P0"],
+                           seed=31)
+    gd = GlobalData.from_infile(w.write_infile(str(tmp_path)))
+    V, peram, noise = workload_inputs(w)
+    rng = np.random.default_rng(12)
+    U = [_random_links(rng, 64) for _ in range(w.Lt)]
+
+    def run(slots_, precision):
+        eng = Engine(gd.dims)
+        eng.set_operators(gd.plan)
+        if slots_:
+            eng.set_eigenvector_slots(slots_)
+        for t, v in enumerate(V):
+            eng.set_eigenvectors(t, v)
+        for r, p in enumerate(peram):
+            eng.set_perambulator(r, p)
+        for r in range(noise.shape[0]):
+            eng.set_random_vector(r, noise[r])
+        for t, u in enumerate(U):
+            eng.set_gauge(t, u)
+        eng.vdaggerv_build(precision)
+        blocks = [eng.vdaggerv_fetch(o, t) for o in range(gd.plan.n_vdv_ops) for t in range(w.Lt)]
+        return blocks, eng.contract(gd.plan_ptr, precision, 0)
+
+    for precision in (0, 1):
+        b0, c0 = run(0, precision)
+        b1, c1 = run(slots, precision)
+        for x, y in zip(b0, b1):
+            np.testing.assert_array_equal(x, y)
+        np.testing.assert_array_equal(c0, c1)
+        assert np.max(np.abs(c0)) > 0
+
+
+def test_streamed_eigenvectors_need_every_timeslice(l4):
+    from slaph_gb300._lib import SlaphError, SLAPH_ERR_STATE
+    from slaph_gb300.engine import Engine
+    eng = Engine(l4["gd"].dims)
+    eng.set_operators(l4["gd"].plan)
+    eng.set_eigenvector_slots(2)
+    eng.set_eigenvectors(0, l4["V"][0])
+    with pytest.raises(SlaphError) as ei:
+        eng.vdaggerv_build(1)
+    assert ei.value.code == SLAPH_ERR_STATE

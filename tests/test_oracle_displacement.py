@@ -84,3 +84,33 @@ def test_displaced_vdaggerv_matches_reference_loop(engine_lib, oracle_lib, tmp_p
             ref = Vt.conj().T @ displace(Vt, U[t], steps, iup, idn)
             np.testing.assert_allclose(got[o, t].T, ref, rtol=0, atol=1e-13)
     assert n_disp == len(ops)
+
+
+def test_double_double_columns_match_the_fp64_oracle(engine_lib, oracle_lib, tmp_path):
+    """The oracle's double-double VdaggerV columns (the large-K reference of
+    the GPU tests) against its FP64 blocks on a small lattice, momentum and
+    displaced operators."""
+    from oracle import frontend
+    from slaph_gb300 import synthetic
+    w = synthetic.Workload("dd", Lt=2, L=4, nev=6, n_rnd=2, dilT=1, dilE=2,
+                           operators=["g5.d0.p0,1", "g5.d>x|<z.p0"],
+                           correlators=["C2c:Q0:Op0:Q0:Op0:P0", "C2c:Q0:Op1:Q0:Op1:P0"], seed=3)
+    gd = frontend.GlobalData(w.write_infile(str(tmp_path)))
+    d = gd.dims
+    rng = np.random.default_rng(2)
+    U = [np.ascontiguousarray(random_links(rng, 64).transpose(0, 1, 3, 2)) for _ in range(d.Lt)]
+    V = [w.eigenvectors(t) for t in range(d.Lt)]
+    ref = oracle.vdaggerv(d, gd.plan, V, U=U)
+    cols = [0, 5]
+    for o in range(gd.plan.n_vdv_ops):
+        op = gd.plan.vdv_ops[o]
+        if o == gd.plan.index_of_unity:
+            continue
+        for t in range(d.Lt):
+            if op.n_disp:
+                W = oracle.displace_eigenvectors(d, op, V[t], U[t])
+                dd = oracle.vdaggerv_columns_dd_w(d, V[t], W, cols)
+            else:
+                dd = oracle.vdaggerv_columns_dd(d, tuple(op.momentum), V[t], cols)
+            for c, j in enumerate(cols):
+                np.testing.assert_allclose(dd[c], ref[o, t][j], rtol=0, atol=1e-14)
