@@ -231,6 +231,8 @@ def run_engine(args):
     slots = args.eigenvector_slots if args.eigenvector_slots >= 0 else w.eigenvector_slots
     if slots > 0:
         eng.set_eigenvector_slots(slots)  # streamed: the builds copy from V
+    if w.factors_per_block_pair:
+        eng.set_factor_lifetime(True)
     # Displaced operators: gauge links of every timeslice, uploaded and
     # HYP-smeared (infile alpha1, alpha2, iterations) per configuration, as
     # create_operators reads and smears them (src/OperatorFactory.cpp:248-260).
@@ -468,6 +470,7 @@ def run_engine(args):
         "device_memory_used_gb": mem_hw,
         "eigenvectors": (f"streamed through {slots} device slots" if slots > 0
                          else "resident (all timeslices)"),
+        "factor_lifetime": "block pair" if w.factors_per_block_pair else "configuration",
 
         "roofline": roofline, "roofline_others": others, "kernels_ms": kernels_ms,
         "clocks": clocks,

@@ -53,6 +53,15 @@ enum slaph_precision {
                       relative (tested at 1e-10)                                */
 };
 
+/* How long the diluted factors of a contraction live (slaph_engine_set_factor_lifetime). */
+enum slaph_factor_lifetime {
+  SLAPH_FACTORS_CONFIGURATION = 0, /* built once per configuration and kept for
+                                      every block pair (the default)           */
+  SLAPH_FACTORS_BLOCK_PAIR = 1     /* built per block pair and dropped after it,
+                                      as the reference clears its factor caches
+                                      per block pair (src/Correlators.cpp:116)  */
+};
+
 enum slaph_accumulator {
   SLAPH_ACC_NATIVE = 0, /* NativeAccumulator (include/KahanAccumulator.hpp:50-72) */
   SLAPH_ACC_KAHAN = 1   /* KahanAccumulator  (include/KahanAccumulator.hpp:14-48) */
@@ -262,6 +271,18 @@ int slaph_engine_set_eigenvectors(slaph_engine *eng, int32_t t, const double *V)
  * n_slots = 0 returns to all timeslices resident (the default).  Earlier
  * eigenvector uploads and VdaggerV are discarded by a change. */
 int slaph_engine_set_eigenvector_slots(slaph_engine *eng, int32_t n_slots);
+
+/* Factor lifetime of the following contractions (enum slaph_factor_lifetime).
+ * With SLAPH_FACTORS_CONFIGURATION every diluted factor of the configuration
+ * is built once and kept, which is fastest but needs device memory for all of
+ * them (two double-float layouts of (4 dilE)^2 entries each: about 60 GB at
+ * 32^3 x 64 pipi I=1, 207 GB at 48^3 x 96 with pipi I=1 + KK).  With
+ * SLAPH_FACTORS_BLOCK_PAIR the contraction runs block pair by block pair, each
+ * with the factors it uses, built for it and dropped after it, as the
+ * reference's DiagramParts caches are (src/Correlators.cpp:69-116): factors
+ * used by several block pairs are built several times, device memory holds
+ * one block pair's.  Correlators are summed in the same order either way. */
+int slaph_engine_set_factor_lifetime(slaph_engine *eng, int mode);
 int slaph_engine_set_perambulator(slaph_engine *eng, int32_t rnd_id, const double *peram);
 int slaph_engine_set_random_vector(slaph_engine *eng, int32_t rnd_id, const double *noise);
 int slaph_engine_set_eigenvectors_async(slaph_engine *eng, int32_t t, const double *V);

@@ -67,6 +67,10 @@ int slaph_engine_set_eigenvector_slots(slaph_engine *eng, int32_t n_slots) {
   return slaph::guarded([&] { get(eng).set_eigenvector_slots(n_slots); });
 }
 
+int slaph_engine_set_factor_lifetime(slaph_engine *eng, int mode) {
+  return slaph::guarded([&] { get(eng).set_factor_lifetime(mode); });
+}
+
 int slaph_engine_set_time_dilution(slaph_engine *eng, int32_t dilT) {
   return slaph::guarded([&] { get(eng).set_time_dilution(dilT); });
 }

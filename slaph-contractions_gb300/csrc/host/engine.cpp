@@ -250,6 +250,8 @@ void Engine::set_time_dilution(int32_t dilT) {
   std::fill(pend_p_.begin(), pend_p_.end(), 0);
   sched_.reset();
   sched_plan_ = nullptr;
+  bp_scheds_.clear();
+  bp_plan_ = nullptr;
 }
 
 void Engine::set_gauge(int32_t t, double const *U) {
@@ -586,6 +588,18 @@ void Engine::vdaggerv_fetch(int32_t op, int32_t t, double *out) {
 void Engine::prepare_schedule(slaph_plan const *plan, int bp) {
   if (sched_ && sched_plan_ == plan && sched_bp_ == bp) return;
   sched_.reset();
+  sched_ = make_schedule(plan, bp);
+  sched_plan_ = plan;
+  sched_bp_ = bp;
+}
+
+void Engine::set_factor_lifetime(int mode) {
+  if (mode != SLAPH_FACTORS_CONFIGURATION && mode != SLAPH_FACTORS_BLOCK_PAIR)
+    throw ArgError("unknown factor lifetime");
+  factor_lifetime_ = mode;
+}
+
+std::unique_ptr<DeviceSchedule> Engine::make_schedule(slaph_plan const *plan, int bp) {
   auto const t0 = std::chrono::steady_clock::now();
   auto ds = std::make_unique<DeviceSchedule>();
   ds->s = build_schedule(dims_, *plan, bp);
@@ -649,9 +663,7 @@ void Engine::prepare_schedule(slaph_plan const *plan, int bp) {
   SLAPH_CK(cudaStreamSynchronize(stream_));
   ds->plan_seconds =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  sched_ = std::move(ds);
-  sched_plan_ = plan;
-  sched_bp_ = bp;
+  return ds;
 }
 
 // Tensor-core plan of the dense trace groups: per group, one A region per
@@ -1181,16 +1193,31 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   // launches_ continues the count of the preceding VdaggerV build: one gauge
   // configuration = build + contract.
   auto const tp = std::chrono::steady_clock::now();
-  prepare_schedule(plan, single_block_pair);
+  // The schedules to run: one for the whole configuration (factors built once
+  // and kept for every block pair), or one per block pair (factors built for
+  // that block pair and dropped after it, as the reference clears its factor
+  // caches per block pair, src/Correlators.cpp:116); the correlator sums run
+  // over the block pairs in the same order either way.
+  std::vector<DeviceSchedule *> scheds;
+  if (factor_lifetime_ == SLAPH_FACTORS_BLOCK_PAIR) {
+    if (bp_plan_ != plan) {
+      bp_scheds_.clear();
+      bp_plan_ = plan;
+    }
+    int const nb = dims_.Lt / dims_.dilT;
+    for (int b = 0; b < nb * (nb + 1) / 2; ++b) {
+      if (single_block_pair >= 0 && b != single_block_pair) continue;
+      auto &sp = bp_scheds_[b];
+      if (!sp) sp = make_schedule(plan, b);
+      scheds.push_back(sp.get());
+    }
+    if (scheds.empty()) throw ArgError("block pair out of range");
+  } else {
+    prepare_schedule(plan, single_block_pair);
+    scheds.push_back(sched_.get());
+  }
   double const plan_wall =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
-  DeviceSchedule &ds = *sched_;
-  Schedule const &s = ds.s;
-  int32_t const eds = s.eds;
-  int64_t const ms = static_cast<int64_t>(eds) * eds;
-  int64_t const nev = dims_.nev;
-
-  // ---- factors
   bool const mixed = precision == SLAPH_MIXED;
   // Perambulators and noise uploaded asynchronously are waited for here.
   for (int32_t r = 0; r < dims_.n_rnd; ++r) {
@@ -1199,221 +1226,248 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   }
   std::fill(pend_p_.begin(), pend_p_.end(), 0);
   std::fill(pend_n_.begin(), pend_n_.end(), 0);
-  SLAPH_CK(cudaEventRecord(ev_[0], stream_));
-  if (!mixed) {
-    slots_.reserve(sizeof(double2) * ms *
-                   std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots));
-    DevBuf q0m, q1r, q2m;
-    q0m.reserve(sizeof(double2) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
-    q1r.reserve(sizeof(double2) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
-    q2m.reserve(sizeof(double2) * std::max<int64_t>(1, s.q2m.size()) * eds * 4 * nev);
-    double2 const *vdv = vdv_.as<double2>();
-    launch(dev::q0m(q0m.as<double2>(), ds.q0m.as<dev::Q0MInst>(), s.q0m.size(), vdv,
-                    noise_.as<double2>(), geo_, stream_),
-           "q0m");
-    launch(dev::q1r(q1r.as<double2>(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(), vdv,
-                    noise_.as<double2>(), geo_, stream_),
-           "q1r");
-    launch(dev::q2m(q2m.as<double2>(), ds.q2m.as<dev::Q2MInst>(), s.q2m.size(), vdv,
-                    peram_.as<double2>(), geo_, stream_),
-           "q2m");
-    launch(dev::q0(slots_.as<double2>(), ds.q0.as<dev::Q0Inst>(), s.q0.size(),
-                   q0m.as<double2>(), noise_.as<double2>(), geo_, stream_),
-           "q0");
-    launch(dev::q1(slots_.as<double2>(), ds.q1.as<dev::Q1Inst>(), s.q1.size(),
-                   q1r.as<double2>(), peram_.as<double2>(), geo_, stream_),
-           "q1");
-    launch(dev::q2(slots_.as<double2>(), ds.q2.as<dev::Q2Inst>(), s.q2.size(),
-                   q2m.as<double2>(), peram_.as<double2>(), geo_, stream_),
-           "q2");
-    SLAPH_CK(cudaEventRecord(ev_[1], stream_));
-    SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
-  } else {
-    // Double-float matrices in both layouts: factors now, products per wave.
-    size_t const df_bytes =
-        sizeof(float4) * ms * std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots);
-    df_slots_.reserve(df_bytes);
-    df_slots_t_.reserve(df_bytes);
-    int64_t const n_vdv = 2LL * static_cast<int64_t>(ops_.size()) * dims_.Lt * nev * nev;
-    int64_t const n_noise = 4LL * nev * dims_.Lt * dims_.n_rnd;
-    DevBuf vdv_df, noise_df, q0m, q1r;
-    vdv_df.reserve(sizeof(float4) * std::max<int64_t>(1, n_vdv));
-    noise_df.reserve(sizeof(float4) * n_noise);
-    launch(dev::to_df(vdv_df.as<float4>(), vdv_.as<double2>(), n_vdv, stream_), "to_df");
-    launch(dev::to_df(noise_df.as<float4>(), noise_.as<double2>(), n_noise, stream_), "to_df");
-    q0m.reserve(sizeof(float4) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
-    q1r.reserve(sizeof(float4) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
-    // Q0 and the Q1R intermediates in double-float; Q2M, Q1 and Q2 on the
-    // tensor cores below.
-    launch(dev::factors_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), q0m.as<float4>(),
-                           q1r.as<float4>(), nullptr, ds.q0m.as<dev::Q0MInst>(),
-                           s.q0m.size(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(), nullptr, 0,
-                           ds.q0.as<dev::Q0Inst>(), s.q0.size(), nullptr, 0, nullptr, 0,
-                           vdv_df.as<float4>(), noise_df.as<float4>(), nullptr, geo_, stream_),
-           "factors_df");
-    launches_ += 2;
-    prepare_factor_tc(ds);
-    tc_scratch_.reserve(std::max<size_t>(1, ds.f_scratch));
-    f_out_.reserve(sizeof(double2) * std::max<int64_t>(1, ds.f_out));
-    tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, ds.f_expo));
-    err_.reserve(sizeof(int));
-    SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
-    int32_t const kt1 = dev::gemm_k_tiles(nev), kt2 = dev::gemm_k_tiles(4 * nev);
-    uint8_t *scr = tc_scratch_.as<uint8_t>();
-    int32_t *ex = tr_expo_.as<int32_t>();
-    double2 *fo = f_out_.as<double2>();
-    auto const *fv = ds.fvec.as<dev::GVec>();
-    auto const *ft = ds.ftiles.as<dev::TrTile>();
-    auto count = [&](int64_t n) { launches_ += n > 0 ? 1 : 0; };
-    for (auto const &b : ds.f_batches) {
-      cuda_check(dev::gvec_slice_df(scr, ex, fv + b.a_x1[0], b.a_x1[1], true, true,
-                                    q1r.as<float4>(), kt1, stream_),
-                 "slice X1 A");
-      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.a_q2m[0], b.a_q2m[1], true, false,
-                                     peram_.as<double2>(), kt1, stream_),
-                 "slice Q2M A");
-      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_x1[0], b.b_x1[1], false, false,
-                                     peram_.as<double2>(), kt1, stream_),
-                 "slice X1 B");
-      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_q2m[0], b.b_q2m[1], false, false,
-                                     vdv_.as<double2>(), kt1, stream_),
-                 "slice Q2M B");
-      count(b.a_x1[1]); count(b.a_q2m[1]); count(b.b_x1[1]); count(b.b_q2m[1]);
-      cuda_check(dev::tc_gemm(fo, scr, ex, ft + b.t1[0], b.t1[1], kt1, err_.as<int>(), stream_),
-                 "factor GEMM (X1, Q2M)");
-      count(b.t1[1]);
-      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.a_q2[0], b.a_q2[1], true, true, fo, kt2,
-                                     stream_),
-                 "slice Q2 A");
-      cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_q2[0], b.b_q2[1], false, false,
-                                     peram_.as<double2>(), kt2, stream_),
-                 "slice Q2 B");
-      count(b.a_q2[1]); count(b.b_q2[1]);
-      cuda_check(dev::tc_gemm(fo, scr, ex, ft + b.t2[0], b.t2[1], kt2, err_.as<int>(), stream_),
-                 "factor GEMM (Q2)");
-      count(b.t2[1]);
-      cuda_check(dev::q1_gather(df_slots_.as<float4>(), df_slots_t_.as<float4>(),
-                                ds.fg1.as<dev::Q1Gather>() + b.g1[0], b.g1[1], fo, dims_.dilE,
-                                stream_),
-                 "q1_gather");
-      cuda_check(dev::q2_gather(df_slots_.as<float4>(), df_slots_t_.as<float4>(),
-                                ds.fg2.as<dev::Q2Gather>() + b.g2[0], b.g2[1], fo, eds, stream_),
-                 "q2_gather");
-      count(b.g1[1]); count(b.g2[1]);
-    }
-    SLAPH_CK(cudaEventRecord(ev_[1], stream_));
-    SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
-  }
-  timings[1] = elapsed_ms(ev_[0], ev_[1]);
-  // Perambulators and noise are not read after the factor stage.
-  SLAPH_CK(cudaEventRecord(ev_pn_used_, stream_));
-
-  // ---- waves: products, traces, terms, accumulation
-  values_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_values));
-  term_val_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_terms));
-  int64_t const n_run = std::max<int64_t>(1, s.n_outputs * dims_.Lt);
+  int64_t const n_outputs = scheds.front()->s.n_outputs;
+  int64_t const n_run = std::max<int64_t>(1, n_outputs * dims_.Lt);
   running_.reserve(sizeof(double2) * n_run);
   SLAPH_CK(cudaMemsetAsync(running_.as<void>(), 0, sizeof(double2) * n_run, stream_));
-  double t_pt = 0, t_as = 0, t_tr = 0, t_sl = 0, t_gm = 0;
+  double t_f = 0, t_pt = 0, t_as = 0, t_tr = 0, t_sl = 0, t_gm = 0;
   int64_t n_tr = 0, n_gm = 0;
-  if (mixed) {
-    prepare_trace_tc(ds);
-    tc_scratch_.reserve(std::max<size_t>(1, ds.tc_scratch));
-    tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, ds.tc_expo));
-    err_.reserve(sizeof(int));
-    SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
-  }
-  for (size_t wi = 0; wi < s.waves.size(); ++wi) {
-    Wave const &w = s.waves[wi];
-    auto &wb = *ds.waves[wi];
-    SLAPH_CK(cudaEventRecord(ev_[2], stream_));
-    auto const *prods = wb.prods.as<dev::ProdInst>();
-    for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
-      int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
-      if (e <= b) continue;
-      if (mixed)
-        launch(dev::products_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), prods + b,
-                                e - b, eds, stream_),
-               "products_df");
-      else
-        launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
-    }
-    int64_t const n_res = static_cast<int64_t>(w.residual_lists.size());
-    int64_t const n_uni = static_cast<int64_t>(w.unique_lists.size());
-    SLAPH_CK(cudaEventRecord(ev_[5], stream_));
-    if (mixed) {
-      values_df_.reserve(sizeof(float4) * std::max<int64_t>(1, s.max_values));
-      if (n_res > 0)
-        launch(dev::traces_df(values_df_.as<float4>(), wb.lists.as<dev::TraceList>(),
-                              wb.residual.as<int32_t>(), n_res, ds.shape_i.as<int32_t>(),
-                              ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
-                              df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds, stream_),
-               "traces_df");
-      SLAPH_CK(cudaEventRecord(ev_[6], stream_));
-      int64_t const gv = w.n_group_values;
-      if (w.n_values > gv)
-        launch(dev::df_values_to_fp64(values_.as<double2>() + gv, values_df_.as<float4>() + gv,
-                                      w.n_values - gv, stream_),
-               "df_values_to_fp64");
-      // Dense groups on the tensor cores: slice, then GEMM, per batch.
-      while (tc_ev_.size() < 3 * wb.tc_batches.size()) {
-        cudaEvent_t e = nullptr;
-        SLAPH_CK(cudaEventCreate(&e));
-        tc_ev_.push_back(e);
-      }
-      for (size_t bi = 0; bi < wb.tc_batches.size(); ++bi) {
-        auto const &b = wb.tc_batches[bi];
-        SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi], stream_));
-        cuda_check(dev::trace_tc_slice(tc_scratch_.as<uint8_t>(), tr_expo_.as<int32_t>(),
-                                       wb.tc_a.as<dev::TrSlice>() + b.a_off, b.n_a,
-                                       wb.tc_b.as<dev::TrSlice>() + b.b_off, b.n_b,
-                                       df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds,
-                                       stream_),
-                   "trace_tc_slice");
-        launches_ += (b.n_a > 0 ? 1 : 0) + (b.n_b > 0 ? 1 : 0);
-        SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 1], stream_));
-        launch(dev::trace_tc_gemm(values_.as<double2>(), tc_scratch_.as<uint8_t>(),
-                                  tr_expo_.as<int32_t>(), wb.tc_tiles.as<dev::TrTile>() + b.tile_off,
-                                  b.n_tiles, eds, err_.as<int>(), stream_),
-               "trace_tc_gemm");
-        SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 2], stream_));
-      }
+  double st[8] = {};
+  for (DeviceSchedule *dsp : scheds) {
+    DeviceSchedule &ds = *dsp;
+    Schedule const &s = ds.s;
+    int32_t const eds = s.eds;
+    int64_t const ms = static_cast<int64_t>(eds) * eds;
+    int64_t const nev = dims_.nev;
+
+    // ---- factors
+    SLAPH_CK(cudaEventRecord(ev_[0], stream_));
+    if (!mixed) {
+      slots_.reserve(sizeof(double2) * ms *
+                     std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots));
+      DevBuf q0m, q1r, q2m;
+      q0m.reserve(sizeof(double2) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
+      q1r.reserve(sizeof(double2) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
+      q2m.reserve(sizeof(double2) * std::max<int64_t>(1, s.q2m.size()) * eds * 4 * nev);
+      double2 const *vdv = vdv_.as<double2>();
+      launch(dev::q0m(q0m.as<double2>(), ds.q0m.as<dev::Q0MInst>(), s.q0m.size(), vdv,
+                      noise_.as<double2>(), geo_, stream_),
+             "q0m");
+      launch(dev::q1r(q1r.as<double2>(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(), vdv,
+                      noise_.as<double2>(), geo_, stream_),
+             "q1r");
+      launch(dev::q2m(q2m.as<double2>(), ds.q2m.as<dev::Q2MInst>(), s.q2m.size(), vdv,
+                      peram_.as<double2>(), geo_, stream_),
+             "q2m");
+      launch(dev::q0(slots_.as<double2>(), ds.q0.as<dev::Q0Inst>(), s.q0.size(),
+                     q0m.as<double2>(), noise_.as<double2>(), geo_, stream_),
+             "q0");
+      launch(dev::q1(slots_.as<double2>(), ds.q1.as<dev::Q1Inst>(), s.q1.size(),
+                     q1r.as<double2>(), peram_.as<double2>(), geo_, stream_),
+             "q1");
+      launch(dev::q2(slots_.as<double2>(), ds.q2.as<dev::Q2Inst>(), s.q2.size(),
+                     q2m.as<double2>(), peram_.as<double2>(), geo_, stream_),
+             "q2");
+      SLAPH_CK(cudaEventRecord(ev_[1], stream_));
+      SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
     } else {
-      if (n_uni > 0)
-        launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
-                           wb.unique.as<int32_t>(), n_uni, ds.shape_i.as<int32_t>(),
-                           ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
-                           slots_.as<double2>(), eds, stream_),
-               "traces");
-      SLAPH_CK(cudaEventRecord(ev_[6], stream_));
-    }
-    bool const traced = mixed ? n_res > 0 : n_uni > 0;
-    SLAPH_CK(cudaEventRecord(ev_[3], stream_));
-    launch(dev::terms(term_val_.as<double2>(), wb.terms.as<dev::Term>(),
-                      static_cast<int64_t>(w.terms.size()), wb.lists.as<dev::TraceList>(),
-                      values_.as<double2>(), ds.shape_mask.as<uint16_t>(),
-                      ds.shape_off.as<int64_t>(), accumulator == SLAPH_ACC_KAHAN ? 1 : 0,
-                      stream_),
-           "terms");
-    launch(dev::accumulate(running_.as<double2>(), wb.seg_out.as<int32_t>(),
-                           wb.seg_off.as<int64_t>(), wb.n_seg, wb.idx.as<int32_t>(),
-                           term_val_.as<double2>(), stream_),
-           "accumulate");
-    SLAPH_CK(cudaEventRecord(ev_[4], stream_));
-    SLAPH_CK(cudaEventSynchronize(ev_[4]));
-    t_pt += elapsed_ms(ev_[2], ev_[3]);
-    t_as += elapsed_ms(ev_[3], ev_[4]);
-    if (traced) {
-      t_tr += elapsed_ms(ev_[5], ev_[6]);
-      ++n_tr;
-    }
-    if (mixed)
-      for (size_t bi = 0; bi < wb.tc_batches.size(); ++bi) {
-        t_sl += elapsed_ms(tc_ev_[3 * bi], tc_ev_[3 * bi + 1]);
-        t_gm += elapsed_ms(tc_ev_[3 * bi + 1], tc_ev_[3 * bi + 2]);
-        ++n_gm;
+      // Double-float matrices in both layouts: factors now, products per wave.
+      size_t const df_bytes =
+          sizeof(float4) * ms * std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots);
+      df_slots_.reserve(df_bytes);
+      df_slots_t_.reserve(df_bytes);
+      int64_t const n_vdv = 2LL * static_cast<int64_t>(ops_.size()) * dims_.Lt * nev * nev;
+      int64_t const n_noise = 4LL * nev * dims_.Lt * dims_.n_rnd;
+      DevBuf vdv_df, noise_df, q0m, q1r;
+      vdv_df.reserve(sizeof(float4) * std::max<int64_t>(1, n_vdv));
+      noise_df.reserve(sizeof(float4) * n_noise);
+      launch(dev::to_df(vdv_df.as<float4>(), vdv_.as<double2>(), n_vdv, stream_), "to_df");
+      launch(dev::to_df(noise_df.as<float4>(), noise_.as<double2>(), n_noise, stream_), "to_df");
+      q0m.reserve(sizeof(float4) * std::max<int64_t>(1, s.q0m.size()) * nev * eds);
+      q1r.reserve(sizeof(float4) * std::max<int64_t>(1, s.q1r.size()) * nev * eds);
+      // Q0 and the Q1R intermediates in double-float; Q2M, Q1 and Q2 on the
+      // tensor cores below.
+      launch(dev::factors_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), q0m.as<float4>(),
+                             q1r.as<float4>(), nullptr, ds.q0m.as<dev::Q0MInst>(),
+                             s.q0m.size(), ds.q1r.as<dev::Q1RInst>(), s.q1r.size(), nullptr, 0,
+                             ds.q0.as<dev::Q0Inst>(), s.q0.size(), nullptr, 0, nullptr, 0,
+                             vdv_df.as<float4>(), noise_df.as<float4>(), nullptr, geo_, stream_),
+             "factors_df");
+      launches_ += 2;
+      prepare_factor_tc(ds);
+      tc_scratch_.reserve(std::max<size_t>(1, ds.f_scratch));
+      f_out_.reserve(sizeof(double2) * std::max<int64_t>(1, ds.f_out));
+      tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, ds.f_expo));
+      err_.reserve(sizeof(int));
+      SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
+      int32_t const kt1 = dev::gemm_k_tiles(nev), kt2 = dev::gemm_k_tiles(4 * nev);
+      uint8_t *scr = tc_scratch_.as<uint8_t>();
+      int32_t *ex = tr_expo_.as<int32_t>();
+      double2 *fo = f_out_.as<double2>();
+      auto const *fv = ds.fvec.as<dev::GVec>();
+      auto const *ft = ds.ftiles.as<dev::TrTile>();
+      auto count = [&](int64_t n) { launches_ += n > 0 ? 1 : 0; };
+      for (auto const &b : ds.f_batches) {
+        cuda_check(dev::gvec_slice_df(scr, ex, fv + b.a_x1[0], b.a_x1[1], true, true,
+                                      q1r.as<float4>(), kt1, stream_),
+                   "slice X1 A");
+        cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.a_q2m[0], b.a_q2m[1], true, false,
+                                       peram_.as<double2>(), kt1, stream_),
+                   "slice Q2M A");
+        cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_x1[0], b.b_x1[1], false, false,
+                                       peram_.as<double2>(), kt1, stream_),
+                   "slice X1 B");
+        cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_q2m[0], b.b_q2m[1], false, false,
+                                       vdv_.as<double2>(), kt1, stream_),
+                   "slice Q2M B");
+        count(b.a_x1[1]); count(b.a_q2m[1]); count(b.b_x1[1]); count(b.b_q2m[1]);
+        cuda_check(dev::tc_gemm(fo, scr, ex, ft + b.t1[0], b.t1[1], kt1, err_.as<int>(), stream_),
+                   "factor GEMM (X1, Q2M)");
+        count(b.t1[1]);
+        cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.a_q2[0], b.a_q2[1], true, true, fo, kt2,
+                                       stream_),
+                   "slice Q2 A");
+        cuda_check(dev::gvec_slice_f64(scr, ex, fv + b.b_q2[0], b.b_q2[1], false, false,
+                                       peram_.as<double2>(), kt2, stream_),
+                   "slice Q2 B");
+        count(b.a_q2[1]); count(b.b_q2[1]);
+        cuda_check(dev::tc_gemm(fo, scr, ex, ft + b.t2[0], b.t2[1], kt2, err_.as<int>(), stream_),
+                   "factor GEMM (Q2)");
+        count(b.t2[1]);
+        cuda_check(dev::q1_gather(df_slots_.as<float4>(), df_slots_t_.as<float4>(),
+                                  ds.fg1.as<dev::Q1Gather>() + b.g1[0], b.g1[1], fo, dims_.dilE,
+                                  stream_),
+                   "q1_gather");
+        cuda_check(dev::q2_gather(df_slots_.as<float4>(), df_slots_t_.as<float4>(),
+                                  ds.fg2.as<dev::Q2Gather>() + b.g2[0], b.g2[1], fo, eds, stream_),
+                   "q2_gather");
+        count(b.g1[1]); count(b.g2[1]);
       }
+      SLAPH_CK(cudaEventRecord(ev_[1], stream_));
+      SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
+    }
+    t_f += elapsed_ms(ev_[0], ev_[1]);
+
+    // ---- waves: products, traces, terms, accumulation
+    values_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_values));
+    term_val_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_terms));
+    if (mixed) {
+      prepare_trace_tc(ds);
+      tc_scratch_.reserve(std::max<size_t>(1, ds.tc_scratch));
+      tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, ds.tc_expo));
+      err_.reserve(sizeof(int));
+      SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
+    }
+    for (size_t wi = 0; wi < s.waves.size(); ++wi) {
+      Wave const &w = s.waves[wi];
+      auto &wb = *ds.waves[wi];
+      SLAPH_CK(cudaEventRecord(ev_[2], stream_));
+      auto const *prods = wb.prods.as<dev::ProdInst>();
+      for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
+        int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
+        if (e <= b) continue;
+        if (mixed)
+          launch(dev::products_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), prods + b,
+                                  e - b, eds, stream_),
+                 "products_df");
+        else
+          launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
+      }
+      int64_t const n_res = static_cast<int64_t>(w.residual_lists.size());
+      int64_t const n_uni = static_cast<int64_t>(w.unique_lists.size());
+      SLAPH_CK(cudaEventRecord(ev_[5], stream_));
+      if (mixed) {
+        values_df_.reserve(sizeof(float4) * std::max<int64_t>(1, s.max_values));
+        if (n_res > 0)
+          launch(dev::traces_df(values_df_.as<float4>(), wb.lists.as<dev::TraceList>(),
+                                wb.residual.as<int32_t>(), n_res, ds.shape_i.as<int32_t>(),
+                                ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
+                                df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds, stream_),
+                 "traces_df");
+        SLAPH_CK(cudaEventRecord(ev_[6], stream_));
+        int64_t const gv = w.n_group_values;
+        if (w.n_values > gv)
+          launch(dev::df_values_to_fp64(values_.as<double2>() + gv, values_df_.as<float4>() + gv,
+                                        w.n_values - gv, stream_),
+                 "df_values_to_fp64");
+        // Dense groups on the tensor cores: slice, then GEMM, per batch.
+        while (tc_ev_.size() < 3 * wb.tc_batches.size()) {
+          cudaEvent_t e = nullptr;
+          SLAPH_CK(cudaEventCreate(&e));
+          tc_ev_.push_back(e);
+        }
+        for (size_t bi = 0; bi < wb.tc_batches.size(); ++bi) {
+          auto const &b = wb.tc_batches[bi];
+          SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi], stream_));
+          cuda_check(dev::trace_tc_slice(tc_scratch_.as<uint8_t>(), tr_expo_.as<int32_t>(),
+                                         wb.tc_a.as<dev::TrSlice>() + b.a_off, b.n_a,
+                                         wb.tc_b.as<dev::TrSlice>() + b.b_off, b.n_b,
+                                         df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds,
+                                         stream_),
+                     "trace_tc_slice");
+          launches_ += (b.n_a > 0 ? 1 : 0) + (b.n_b > 0 ? 1 : 0);
+          SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 1], stream_));
+          launch(dev::trace_tc_gemm(values_.as<double2>(), tc_scratch_.as<uint8_t>(),
+                                    tr_expo_.as<int32_t>(), wb.tc_tiles.as<dev::TrTile>() + b.tile_off,
+                                    b.n_tiles, eds, err_.as<int>(), stream_),
+                 "trace_tc_gemm");
+          SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 2], stream_));
+        }
+      } else {
+        if (n_uni > 0)
+          launch(dev::traces(values_.as<double2>(), wb.lists.as<dev::TraceList>(),
+                             wb.unique.as<int32_t>(), n_uni, ds.shape_i.as<int32_t>(),
+                             ds.shape_j.as<int32_t>(), ds.shape_off.as<int64_t>(),
+                             slots_.as<double2>(), eds, stream_),
+                 "traces");
+        SLAPH_CK(cudaEventRecord(ev_[6], stream_));
+      }
+      bool const traced = mixed ? n_res > 0 : n_uni > 0;
+      SLAPH_CK(cudaEventRecord(ev_[3], stream_));
+      launch(dev::terms(term_val_.as<double2>(), wb.terms.as<dev::Term>(),
+                        static_cast<int64_t>(w.terms.size()), wb.lists.as<dev::TraceList>(),
+                        values_.as<double2>(), ds.shape_mask.as<uint16_t>(),
+                        ds.shape_off.as<int64_t>(), accumulator == SLAPH_ACC_KAHAN ? 1 : 0,
+                        stream_),
+             "terms");
+      launch(dev::accumulate(running_.as<double2>(), wb.seg_out.as<int32_t>(),
+                             wb.seg_off.as<int64_t>(), wb.n_seg, wb.idx.as<int32_t>(),
+                             term_val_.as<double2>(), stream_),
+             "accumulate");
+      SLAPH_CK(cudaEventRecord(ev_[4], stream_));
+      SLAPH_CK(cudaEventSynchronize(ev_[4]));
+      t_pt += elapsed_ms(ev_[2], ev_[3]);
+      t_as += elapsed_ms(ev_[3], ev_[4]);
+      if (traced) {
+        t_tr += elapsed_ms(ev_[5], ev_[6]);
+        ++n_tr;
+      }
+      if (mixed)
+        for (size_t bi = 0; bi < wb.tc_batches.size(); ++bi) {
+          t_sl += elapsed_ms(tc_ev_[3 * bi], tc_ev_[3 * bi + 1]);
+          t_gm += elapsed_ms(tc_ev_[3 * bi + 1], tc_ev_[3 * bi + 2]);
+          ++n_gm;
+        }
+    }
+    if (mixed) {
+      int code = 0;
+      SLAPH_CK(cudaMemcpy(&code, err_.as<void>(), sizeof(int), cudaMemcpyDeviceToHost));
+      if (code != 0)
+        throw TimeoutError("tensor-core factors or traces: a bounded device wait gave up "
+                           "(stage " + std::to_string(code) + ")");
+    }
+    st[6] += static_cast<double>(s.n_unique_entries);
+    st[7] += static_cast<double>(s.n_group_entries);
+    st[0] += static_cast<double>(s.q0.size() + s.q1.size() + s.q2.size());
+    st[1] += static_cast<double>(s.n_prods);
+    st[2] += static_cast<double>(s.n_trace_entries);
+    st[3] += static_cast<double>(s.n_terms);
+    st[4] += s.flops_factors;
+    st[5] += s.flops_products + s.flops_traces;
   }
+  // Perambulators and noise are not read after the factor stages.
+  SLAPH_CK(cudaEventRecord(ev_pn_used_, stream_));
+  timings[1] = t_f;
   timings[2] = t_pt;
   timings[3] = t_as;
   timings[4] = plan_wall * 1e3;
@@ -1423,16 +1477,9 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   timings[8] = t_gm;
   timings[9] = static_cast<double>(n_gm);
   timings[10] = t_sl;
-  if (mixed) {
-    int code = 0;
-    SLAPH_CK(cudaMemcpy(&code, err_.as<void>(), sizeof(int), cudaMemcpyDeviceToHost));
-    if (code != 0)
-      throw TimeoutError("tensor-core traces: a bounded device wait gave up (stage " +
-                         std::to_string(code) + ")");
-  }
 
   // ---- output: C[t] = correlator[t][i] / Lt (src/Diagram.cpp:141-143)
-  std::vector<double2> host(static_cast<size_t>(s.n_outputs * dims_.Lt));
+  std::vector<double2> host(static_cast<size_t>(n_outputs * dims_.Lt));
   if (!host.empty())
     SLAPH_CK(cudaMemcpyAsync(host.data(), running_.as<double2>(), host.size() * sizeof(double2),
                              cudaMemcpyDeviceToHost, stream_));
@@ -1442,14 +1489,7 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     corr_out[2 * i] = host[i].x / inv;
     corr_out[2 * i + 1] = host[i].y / inv;
   }
-  stats[6] = static_cast<double>(s.n_unique_entries);
-  stats[7] = static_cast<double>(s.n_group_entries);
-  stats[0] = static_cast<double>(s.q0.size() + s.q1.size() + s.q2.size());
-  stats[1] = static_cast<double>(s.n_prods);
-  stats[2] = static_cast<double>(s.n_trace_entries);
-  stats[3] = static_cast<double>(s.n_terms);
-  stats[4] = s.flops_factors;
-  stats[5] = s.flops_products + s.flops_traces;
+  for (int k = 0; k < 8; ++k) stats[k] = st[k];
 }
 
 }  // namespace slaph

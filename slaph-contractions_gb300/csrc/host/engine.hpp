@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -95,6 +96,8 @@ class Engine {
   // n >= 2: a ring of n timeslice slots, filled from the host buffers given to
   // set_eigenvectors during vdaggerv_build, n / 2 timeslices at a time.
   void set_eigenvector_slots(int32_t n);
+  // SLAPH_FACTORS_CONFIGURATION or SLAPH_FACTORS_BLOCK_PAIR.
+  void set_factor_lifetime(int mode);
   // HYP smearing of the stored links of every timeslice, in place.
   void smear_gauge_hyp(double alpha1, double alpha2, int32_t iterations);
   void gauge_fetch(int32_t t, double *out);
@@ -146,9 +149,14 @@ class Engine {
   std::unique_ptr<DeviceSchedule> sched_;
   slaph_plan const *sched_plan_ = nullptr;
   int sched_bp_ = -2;
+  // Factors per block pair: one schedule per block pair of bp_plan_.
+  int factor_lifetime_ = SLAPH_FACTORS_CONFIGURATION;
+  std::map<int, std::unique_ptr<DeviceSchedule>> bp_scheds_;
+  slaph_plan const *bp_plan_ = nullptr;
 
   int64_t peram_elems() const;
   void prepare_schedule(slaph_plan const *plan, int single_block_pair);
+  std::unique_ptr<DeviceSchedule> make_schedule(slaph_plan const *plan, int single_block_pair);
   void prepare_trace_tc(DeviceSchedule &ds);
   void prepare_factor_tc(DeviceSchedule &ds);
   void launch(cudaError_t e, char const *what) {

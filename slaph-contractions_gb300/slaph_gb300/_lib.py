@@ -23,6 +23,8 @@ SLAPH_ERR_TIMEOUT = 9
 
 SLAPH_FP64 = 0
 SLAPH_MIXED = 1
+SLAPH_FACTORS_CONFIGURATION = 0
+SLAPH_FACTORS_BLOCK_PAIR = 1
 SLAPH_ACC_NATIVE = 0
 SLAPH_ACC_KAHAN = 1
 SLAPH_TR_KINDS = 8
@@ -123,6 +125,7 @@ PROTOTYPES = {
     "slaph_engine_set_gauge": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_engine_set_time_dilution": (C.c_int, [C.c_void_p, _i32]),
     "slaph_engine_set_eigenvector_slots": (C.c_int, [C.c_void_p, _i32]),
+    "slaph_engine_set_factor_lifetime": (C.c_int, [C.c_void_p, C.c_int]),
     "slaph_engine_smear_gauge_hyp": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _i32]),
     "slaph_engine_gauge_fetch": (C.c_int, [C.c_void_p, _i32, _dp]),
     "slaph_selftest_bounded_wait": (C.c_int, [_i64, C.POINTER(_i32)]),

@@ -109,6 +109,14 @@ class Engine:
         self._ring = int(n_slots) > 0
         self._keep = {}
 
+    def set_factor_lifetime(self, per_block_pair):
+        """Diluted factors built once per configuration (False, the default) or
+        per block pair and dropped after it (True: device memory for one block
+        pair's factors); see slaph_engine_set_factor_lifetime."""
+        L.check(L.lib().slaph_engine_set_factor_lifetime(
+            self._h, L.SLAPH_FACTORS_BLOCK_PAIR if per_block_pair else
+            L.SLAPH_FACTORS_CONFIGURATION))
+
     def set_time_dilution(self, dilT):
         """Slices per time-dilution block for the following contractions
         (slaph_engine_set_time_dilution); perambulators are uploaded after it."""

@@ -57,6 +57,9 @@ class Workload:
     # > 0: the engine streams the eigenvectors through this many device slots
     # (slaph_engine_set_eigenvector_slots) instead of keeping all resident.
     eigenvector_slots: int = 0
+    # True: factors built per block pair (slaph_engine_set_factor_lifetime),
+    # for workloads whose factors of a whole configuration exceed the device.
+    factors_per_block_pair: bool = False
 
     @property
     def dim_row(self):
@@ -241,7 +244,7 @@ CONFIGS["cfg5_48x96"] = Workload(
                     "C2c:Q0:Op12:Q0:Op12:P0"]),
     quark_lines=("u:6:TB:16:EI:8:DF:4:synthetic", "s:6:TB:16:EI:8:DF:4:synthetic"),
     extra={"alpha1": 0.62, "alpha2": 0.62, "iterations": 3},
-    seed=909, orthonormal=False, v_period=8, eigenvector_slots=2,
+    seed=909, orthonormal=False, v_period=8, eigenvector_slots=2, factors_per_block_pair=True,
     description="48^3x96 Nev=220: pipi I=1 + KK + displaced, streamed eigenvectors")
 
 

@@ -877,3 +877,36 @@ def test_streamed_eigenvectors_need_every_timeslice(l4):
     with pytest.raises(SlaphError) as ei:
         eng.vdaggerv_build(1)
     assert ei.value.code == SLAPH_ERR_STATE
+
+
+# ---------------------------------------------------------------- factors per block pair
+@pytest.mark.parametrize("name", ["pipi_small", "pipi_groups_e4"])
+def test_factors_per_block_pair_match_factors_per_configuration(name, oracle_lib):
+    """slaph_engine_set_factor_lifetime(SLAPH_FACTORS_BLOCK_PAIR): the
+    contraction block pair by block pair, each with the factors it uses (the
+    reference's per-block-pair caches, src/Correlators.cpp:69-116), gives
+    exactly the correlators of factors kept for the whole configuration, in
+    both precisions and accumulators, and the single-block-pair hook works in
+    that mode too."""
+    from slaph_gb300 import synthetic
+    w = synthetic.CONFIGS[name] if name in synthetic.CONFIGS else synthetic.small_pipi()
+    gd, V, peram, noise = _synthetic_case(w)
+    eng = make_engine(gd, V, peram, noise)
+    for precision in (0, 1):
+        eng.vdaggerv_build(precision)
+        for acc in (0, 1):
+            eng.set_factor_lifetime(False)
+            ref = eng.contract(gd.plan_ptr, precision, acc)
+            eng.set_factor_lifetime(True)
+            got = eng.contract(gd.plan_ptr, precision, acc)
+            np.testing.assert_array_equal(got, ref)
+        eng.set_factor_lifetime(False)
+        one = eng.contract(gd.plan_ptr, precision, 0, single_block_pair=1)
+        eng.set_factor_lifetime(True)
+        np.testing.assert_array_equal(eng.contract(gd.plan_ptr, precision, 0,
+                                                   single_block_pair=1), one)
+    vdv = oracle.vdaggerv(og(gd).dims, og(gd).plan, V)
+    ref = oracle.contract(og(gd).dims, og(gd).plan_ptr, vdv, peram, noise, 0, -1,
+                          gd.output_doubles()).reshape(-1, gd.dims.Lt)
+    eng.vdaggerv_build(0)
+    assert corr_rel_err(eng.contract(gd.plan_ptr, 0, 0), ref) < REL_FP64
