@@ -21,15 +21,16 @@
 //   2^-24 of their own magnitude, at most 2^-40 of the row scale.  21 pairs
 //   (p + q <= 7), 6 accumulators.
 // * Promotion.  After every chunk the 6 accumulators are read from TMEM and
-//   added, scaled by 2^-8(l-2), into a double-float (two FP32) accumulator in
+//   added, scaled by 2^-8l, into a double-float (two FP32) accumulator in
 //   registers; FP64 units are not used in the loop.  The result of a tile
 //   entry is (hi + lo) 2^(e_row + e_col - 14).
 //
 // Slices live in global memory already in the tcgen05 K-major core-matrix
 // layout, one contiguous block of kStageA (kStageB) bytes per (tile, k-tile),
 // and are moved to shared memory by bulk asynchronous copies (cp.async.bulk)
-// completing on mbarriers.  Warp roles: warp 4 issues the copies, warp 5
-// issues tcgen05.mma, warps 0-3 promote and hand the result to the epilogue.
+// completing on mbarriers.  Warp roles (ozaki_tiles): one warp issues the
+// copies, one issues tcgen05.mma, eight promote and hand the result to the
+// epilogue; CTAs are persistent over the tiles of a launch.
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // in *err and winds down, and TMEM is always released.
 #pragma once
@@ -56,7 +57,6 @@ constexpr uint32_t kStageBytes = kStageA + kStageB;  // 79872 B
 constexpr uint32_t kSmemBytes = kStages * kStageBytes;
 constexpr uint32_t kTmemCols = 512;
 constexpr int kLevels = 6;  // p + q = 2..7
-constexpr int kThreads = 192;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
 // byte offset of element (r, k) in a K-major, no-swizzle core-matrix tile with
@@ -159,20 +159,6 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
           smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // Error-free x + y into (s, e) (Knuth's two-sum).
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   s = a + b;
@@ -314,22 +300,66 @@ __device__ __forceinline__ int expo_of_max(double m) {
   return e;
 }
 
-// One 128 x 80 output tile of D = A' B^T over k_tiles k-tiles: a_src and b_src
-// point at the tile's kStageA / kStageB blocks (consecutive per k-tile).  Must
-// be called by all kThreads threads with kSmemBytes of dynamic shared memory.
-// The promotion warps (0-3) call epi(row, hi, lo) with row = 32 * warp + lane
-// of the M tile and the double-float (hi, lo) of the row's kTN columns; the
+// The tiles of one launch, each a 128 x 80 output tile of D = A' B^T over
+// k_tiles k-tiles, computed by a persistent CTA: CTA b takes tiles b, b + G,
+// b + 2G, ... (G = gridDim.x, at most one CTA per SM).  src(i, a, b) gives the
+// kStageA / kStageB blocks of tile i (consecutive per k-tile).  Must be called
+// by all kThreads threads with kSmemBytes of dynamic shared memory.
+//
+// Roles: warp kProducerWarp issues the bulk copies, running ahead across tile
+// boundaries; warp kMmaWarp issues tcgen05.mma; promotion warps 0..7 read the
+// level accumulators after every chunk.  A promotion warp w owns TMEM lane
+// quadrant w % 4 (rows 32 (w % 4) + lane) and the kColsW columns from
+// kColsW (w / 4) on.  Once the last chunk of a tile is promoted the
+// accumulators are released, so the MMAs of the next tile run while the
+// promotion warps hand the previous tile to the epilogue: epi(i, row, col0,
+// hi, lo) with the double-float (hi, lo) of the row's kColsW columns; the
 // result is (hi + lo) 2^(e_row + e_col - 14).
-template <typename Epilogue>
-__device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
-                                           uint8_t const *b_src, int k_tiles, int *err,
-                                           Epilogue const &epi) {
+//
+// Chunk value of one column, sum_l E_l 2^-8l: levels 0 and 1 are exact
+// integers in FP32; levels 3..5 (at most 2^-24 of the row scale) are summed in
+// FP32 first, rounding by at most 2^-24 of their own magnitude, then levels 1,
+// 2 and that sum enter through error-free two-sums.
+constexpr int kPromoWarps = 8;
+constexpr int kProducerWarp = kPromoWarps, kMmaWarp = kPromoWarps + 1;
+constexpr int kThreads = 32 * (kPromoWarps + 2);
+constexpr int kColsW = kTN / (kPromoWarps / 4);  // 40
+static_assert(kColsW % 8 == 0, "promotion loads 8 columns at a time");
+
+__device__ __forceinline__ void tmem_ld8_issue(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+}
+// Waits for the TMEM loads of this thread; the loaded registers pass through
+// the wait (and through empty asm statements after it), so that no use of
+// them can be scheduled before the data has arrived.
+template <int N>
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[N][8]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0][0]), "+r"(r[0][1]), "+r"(r[0][2]), "+r"(r[0][3]), "+r"(r[0][4]),
+                 "+r"(r[0][5]), "+r"(r[0][6]), "+r"(r[0][7])
+               :
+               : "memory");
+#pragma unroll
+  for (int l = 1; l < N; ++l)
+    asm volatile(""
+                 : "+r"(r[l][0]), "+r"(r[l][1]), "+r"(r[l][2]), "+r"(r[l][3]), "+r"(r[l][4]),
+                   "+r"(r[l][5]), "+r"(r[l][6]), "+r"(r[l][7]));
+}
+
+template <typename Src, typename Epilogue>
+__device__ __forceinline__ void ozaki_tiles(uint8_t *smem, int n_tiles, int k_tiles,
+                                            Src const &src, int *err, Epilogue const &epi) {
   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages];
   __shared__ __align__(8) uint64_t acc_full, acc_empty, done_bar;
   __shared__ uint32_t tmem_slot;
 
   int const warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   int const n_chunks = (k_tiles + kChunkKT - 1) / kChunkKT;
+  int const first_tile = blockIdx.x, tile_step = gridDim.x;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -337,7 +367,7 @@ __device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
       mbar_init(&empty_bar[s], 1);
     }
     mbar_init(&acc_full, 1);
-    mbar_init(&acc_empty, 4 * 32);
+    mbar_init(&acc_empty, kPromoWarps * 32);
     mbar_init(&done_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -353,129 +383,153 @@ __device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
   tc_fence_after();
   uint32_t const tmem = tmem_slot;
 
-  if (warp == 4) {
-    if (lane == 0) {  // producer
-      int issued = 0;
-      for (int kt = 0; kt < k_tiles; ++kt) {
-        int const s = kt % kStages, use = kt / kStages;
-        if (kt >= kStages && !mbar_wait(&empty_bar[s], (use - 1) & 1, err, 1)) break;
-        uint8_t *dst = smem + s * kStageBytes;
-        mbar_expect_tx(&full_bar[s], kStageBytes);
-        bulk_g2s(dst, a_src + static_cast<int64_t>(kt) * kStageA, kStageA, &full_bar[s]);
-        bulk_g2s(dst + kStageA, b_src + static_cast<int64_t>(kt) * kStageB, kStageB,
-                 &full_bar[s]);
-        issued = kt + 1;
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      int64_t g = 0;  // k-tiles issued over all tiles of this CTA
+      bool ok = true;
+      for (int i = first_tile; i < n_tiles && ok; i += tile_step) {
+        uint8_t const *a_src, *b_src;
+        src(i, a_src, b_src);
+        for (int kt = 0; kt < k_tiles; ++kt, ++g) {
+          int const s = static_cast<int>(g % kStages);
+          uint32_t const use = static_cast<uint32_t>(g / kStages);
+          if (g >= kStages && !mbar_wait(&empty_bar[s], (use - 1) & 1, err, 1)) {
+            ok = false;
+            break;
+          }
+          uint8_t *dst = smem + s * kStageBytes;
+          mbar_expect_tx(&full_bar[s], kStageBytes);
+          bulk_g2s(dst, a_src + static_cast<int64_t>(kt) * kStageA, kStageA, &full_bar[s]);
+          bulk_g2s(dst + kStageA, b_src + static_cast<int64_t>(kt) * kStageB, kStageB,
+                   &full_bar[s]);
+        }
       }
       // The copies of the last stages have landed before shared memory is
       // released (immediate when the MMA warp consumed them).
-      for (int kt = issued > kStages ? issued - kStages : 0; kt < issued; ++kt)
-        mbar_wait(&full_bar[kt % kStages], (kt / kStages) & 1, err, 6);
+      for (int64_t q = g > kStages ? g - kStages : 0; q < g; ++q)
+        mbar_wait(&full_bar[q % kStages], static_cast<uint32_t>(q / kStages) & 1, err, 6);
     }
-  } else if (warp == 5) {
+  } else if (warp == kMmaWarp) {
     if (lane == 0) {  // MMA issuer
       bool ok = true;
-      for (int c = 0; c < n_chunks && ok; ++c) {
-        if (c > 0 && !mbar_wait(&acc_empty, (c - 1) & 1, err, 2)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        bool first = true;  // the chunk's first k-step starts every accumulator
-        int const kt_end = min(k_tiles, (c + 1) * kChunkKT);
-        for (int kt = c * kChunkKT; kt < kt_end; ++kt) {
-          int const s = kt % kStages, use = kt / kStages;
-          if (!mbar_wait(&full_bar[s], use & 1, err, 3)) {
+      int64_t g = 0, c_all = 0;  // k-tiles and chunks consumed over all tiles
+      for (int i = first_tile; i < n_tiles && ok; i += tile_step) {
+        for (int c = 0; c < n_chunks && ok; ++c, ++c_all) {
+          // accumulators free: the previous chunk (of this or the last tile) promoted
+          if (c_all > 0 &&
+              !mbar_wait(&acc_empty, static_cast<uint32_t>(c_all - 1) & 1, err, 2)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          uint32_t const base = smem_u32(smem + s * kStageBytes);
-#pragma unroll
-          for (int ks = 0; ks < kTK / 16; ++ks) {
-            // The 21 slice pairs p + q <= 5 (0-based; 1-based p + q <= 7), as
-            // 9 MMAs: A_p against the B slices q0 .. q0 + nb - 1 into the
-            // level accumulators p + q0 onwards.  Per level the slice pairs
-            // still arrive in increasing p, and the p = 0 MMAs of a chunk's
-            // first k-step (levels 0..5) overwrite instead of accumulating.
-#pragma unroll
-            for (int p = 0; p < kSlices; ++p) {
-#pragma unroll
-              for (int q0 = 0; q0 < kSlices - p; q0 += kLevelGroup) {
-                int const nb = min(kLevelGroup, kSlices - p - q0);
-                uint64_t const ad = smem_desc(base + p * kABlk + ks * 256, 128, 512);
-                uint64_t const bd =
-                    smem_desc(base + kStageA + q0 * kBBlk + ks * 256, 128, 512);
-                uint32_t const acc = (first && p == 0) ? 0u : 1u;
-                mma_bf16(tmem + static_cast<uint32_t>((p + q0) * kTN), ad, bd, acc,
-                         idesc_n(nb * kTN));
-              }
+          bool first = true;  // the chunk's first k-step starts every accumulator
+          int const kt_end = min(k_tiles, (c + 1) * kChunkKT);
+          for (int kt = c * kChunkKT; kt < kt_end; ++kt, ++g) {
+            int const s = static_cast<int>(g % kStages);
+            uint32_t const use = static_cast<uint32_t>(g / kStages);
+            if (!mbar_wait(&full_bar[s], use & 1, err, 3)) {
+              ok = false;
+              break;
             }
-            first = false;
+            tc_fence_after();
+            uint32_t const base = smem_u32(smem + s * kStageBytes);
+#pragma unroll
+            for (int ks = 0; ks < kTK / 16; ++ks) {
+              // The 21 slice pairs p + q <= 5 (0-based; 1-based p + q <= 7), as
+              // 9 MMAs: A_p against the B slices q0 .. q0 + nb - 1 into the
+              // level accumulators p + q0 onwards.  Per level the slice pairs
+              // still arrive in increasing p, and the p = 0 MMAs of a chunk's
+              // first k-step (levels 0..5) overwrite instead of accumulating.
+#pragma unroll
+              for (int p = 0; p < kSlices; ++p) {
+#pragma unroll
+                for (int q0 = 0; q0 < kSlices - p; q0 += kLevelGroup) {
+                  int const nb = min(kLevelGroup, kSlices - p - q0);
+                  uint64_t const ad = smem_desc(base + p * kABlk + ks * 256, 128, 512);
+                  uint64_t const bd =
+                      smem_desc(base + kStageA + q0 * kBBlk + ks * 256, 128, 512);
+                  uint32_t const acc = (first && p == 0) ? 0u : 1u;
+                  mma_bf16(tmem + static_cast<uint32_t>((p + q0) * kTN), ad, bd, acc,
+                           idesc_n(nb * kTN));
+                }
+              }
+              first = false;
+            }
+            mma_commit(&empty_bar[s]);  // stage s free once these MMAs complete
           }
-          mma_commit(&empty_bar[s]);  // stage s free once these MMAs complete
+          if (ok) mma_commit(&acc_full);
         }
-        mma_commit(&acc_full);
       }
       mma_commit(&done_bar);
       mbar_wait(&done_bar, 0, err, 4);
     }
   } else {
-    // Promotion warps 0-3: lane row = 32 * warp + lane of the M tile.
-    float hi[kTN], lo[kTN];
+    // Promotion warps: lane row = 32 (warp % 4) + lane, columns col0 .. col0 + kColsW.
+    int const row = 32 * (warp % 4) + lane;
+    int const col0 = kColsW * (warp / 4);
+    uint32_t const lane_addr =
+        tmem + (static_cast<uint32_t>(32 * (warp % 4)) << 16) + static_cast<uint32_t>(col0);
+    int64_t c_all = 0;
+    bool ok = true;
+    for (int i = first_tile; i < n_tiles && ok; i += tile_step) {
+      float hi[kColsW], lo[kColsW];
 #pragma unroll
-    for (int j = 0; j < kTN; ++j) hi[j] = lo[j] = 0.f;
-    uint32_t const lane_addr = tmem + (static_cast<uint32_t>(32 * warp) << 16);
-    // Waits are decided warp-uniformly: the TMEM loads below must be reached by
-    // all lanes of a warp or by none.
-    auto promote = [&](int c) -> bool {
-      if (!__all_sync(0xffffffffu, mbar_wait(&acc_full, c & 1, err, 5))) return false;
-      tc_fence_after();
-#pragma unroll
-      for (int cb = 0; cb < kTN / 16; ++cb) {
-        // Chunk value sum_l E_l 2^-8l as a double-float (ch, cl): E_2 is exact,
-        // each further level enters through an error-free two-sum.
-        float ch[16], cl[16];
-        {
-          float v[16];
-          tmem_ld16(lane_addr + static_cast<uint32_t>(cb * 16), v);
-#pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            ch[u] = v[u];
-            cl[u] = 0.f;
-          }
+      for (int j = 0; j < kColsW; ++j) hi[j] = lo[j] = 0.f;
+      for (int c = 0; c < n_chunks; ++c, ++c_all) {
+        // Waits are decided warp-uniformly: the TMEM loads below must be
+        // reached by all lanes of a warp or by none.
+        if (!__all_sync(0xffffffffu,
+                        mbar_wait(&acc_full, static_cast<uint32_t>(c_all) & 1, err, 5))) {
+          ok = false;
+          break;
         }
-        for (int l = 1; l < kLevels; ++l) {
-          float const sc = __int_as_float((127 - 8 * l) << 23);  // 2^-8l
-          float v[16];
-          tmem_ld16(lane_addr + static_cast<uint32_t>(l * kTN + cb * 16), v);
+        tc_fence_after();
 #pragma unroll
-          for (int u = 0; u < 16; ++u) {
+        for (int cb = 0; cb < kColsW / 8; ++cb) {
+          // Levels 0..2, then 3..5, eight columns at a time (the registers of
+          // three warps on one SM sub-partition share its 16K).
+          uint32_t const ca = lane_addr + static_cast<uint32_t>(cb * 8);
+          uint32_t r[3][8];
+#pragma unroll
+          for (int l = 0; l < 3; ++l) tmem_ld8_issue(ca + static_cast<uint32_t>(l * kTN), r[l]);
+          tmem_ld_wait(r);
+          float s2[8], xs[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            float s1, x1, x2;
+            two_sum(__uint_as_float(r[0][u]), __uint_as_float(r[1][u]) * 0x1p-8f, s1, x1);
+            two_sum(s1, __uint_as_float(r[2][u]) * 0x1p-16f, s2[u], x2);
+            xs[u] = x1 + x2;
+          }
+#pragma unroll
+          for (int l = 0; l < 3; ++l)
+            tmem_ld8_issue(ca + static_cast<uint32_t>((3 + l) * kTN), r[l]);
+          tmem_ld_wait(r);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            float const low =
+                fmaf(__uint_as_float(r[2][u]), 0x1p-16f,
+                     fmaf(__uint_as_float(r[1][u]), 0x1p-8f, __uint_as_float(r[0][u]))) *
+                0x1p-24f;
+            float s3, x3;
+            two_sum(s2[u], low, s3, x3);
+            // Running (hi, lo) += (s3, xs + x3), renormalised so that
+            // |lo| <= ulp(hi)/2.
+            int const j = cb * 8 + u;
             float s, e;
-            two_sum(ch[u], v[u] * sc, s, e);
-            ch[u] = s;
-            cl[u] += e;
+            two_sum(hi[j], s3, s, e);
+            e += lo[j] + (xs[u] + x3);
+            float const h = s + e;
+            lo[j] = e - (h - s);
+            hi[j] = h;
           }
         }
-        // Running (hi, lo) += (ch, cl), renormalised so that |lo| <= ulp(hi)/2.
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          int const j = cb * 16 + u;
-          float s, e;
-          two_sum(hi[j], ch[u], s, e);
-          e += lo[j] + cl[u];
-          float const h = s + e;
-          lo[j] = e - (h - s);
-          hi[j] = h;
-        }
+        tc_fence_before();
+        mbar_arrive(&acc_empty);
       }
-      tc_fence_before();
-      mbar_arrive(&acc_empty);
-      return true;
-    };
-    for (int c = 0; c < n_chunks; ++c)
-      if (!promote(c)) break;
-    // After a timeout the values are incomplete; *err makes the host discard them.
-    epi(32 * warp + lane, hi, lo);
+      // After a timeout the values are incomplete; *err makes the host discard them.
+      if (ok) epi(i, row, col0, hi, lo);
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -485,6 +539,16 @@ __device__ __forceinline__ void ozaki_tile(uint8_t *smem, uint8_t const *a_src,
                  "r"(kTmemCols)
                  : "memory");
   }
+}
+
+// Persistent grid of a launch of n_tiles tiles: at most one CTA per SM.
+inline int persistent_grid(int64_t n_tiles) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms < 1)
+    sms = 1;
+  return static_cast<int>(n_tiles < sms ? n_tiles : sms);
 }
 
 }  // namespace tc

@@ -12,10 +12,10 @@
 // Operands are double-float matrices (float4 (re_hi, re_lo, im_hi, im_lo)) in
 // the natural (A) and transposed (B) layouts.  trace_slice_kernel cuts one
 // matrix per CTA into the operand stream of its GEMM region, with the
-// matrix's exponent; trace_gemm_kernel computes one 64 x 80 complex output
-// tile per CTA and writes FP64 trace values: the 32 lanes of a warp hold 16
-// consecutive A groups (re, im) of one output column, so the stores of each
-// column are 256 contiguous bytes.
+// matrix's exponent; trace_gemm_kernel computes 64 x 80 complex output tiles
+// (persistent CTAs, one per SM) and writes FP64 trace values: the 32 lanes of
+// a warp hold 16 consecutive A groups (re, im) of one output column, so the
+// stores of each column are 256 contiguous bytes.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -75,30 +75,40 @@ __global__ void __launch_bounds__(kSliceThreads)
 struct TraceEpilogue {
   double *values;
   int32_t const *expo;
-  TrTile t;
-  __device__ __forceinline__ void operator()(int row, float const (&hi)[kTN],
-                                             float const (&lo)[kTN]) const {
+  TrTile const *tiles;
+  __device__ __forceinline__ void operator()(int i, int row, int col0, float const (&hi)[kColsW],
+                                             float const (&lo)[kColsW]) const {
+    TrTile const t = tiles[i];
     int const r = row / 2;
     if (r >= t.rows) return;
     int const er = expo[t.ea + r];
     double *dst = values + 2 * (t.out + r) + (row & 1);
 #pragma unroll
-    for (int c = 0; c < kTN; ++c) {
-      if (c < t.cols)
-        dst[2 * static_cast<int64_t>(c) * t.ld] =
+    for (int c = 0; c < kColsW; ++c) {
+      int const col = col0 + c;
+      if (col < t.cols)
+        dst[2 * static_cast<int64_t>(col) * t.ld] =
             ldexp(static_cast<double>(hi[c]) + static_cast<double>(lo[c]),
-                  er + expo[t.eb + c] - 14);
+                  er + expo[t.eb + col] - 14);
     }
+  }
+};
+
+struct TraceSrc {
+  uint8_t const *scratch;
+  TrTile const *tiles;
+  __device__ __forceinline__ void operator()(int i, uint8_t const *&a, uint8_t const *&b) const {
+    a = scratch + tiles[i].a_src;
+    b = scratch + tiles[i].b_src;
   }
 };
 
 __global__ void __launch_bounds__(kThreads, 1)
     trace_gemm_kernel(double2 *values, uint8_t const *scratch, int32_t const *expo,
-                      TrTile const *tiles, int32_t k_tiles, int *err) {
+                      TrTile const *tiles, int32_t n_tiles, int32_t k_tiles, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  TrTile const t = tiles[blockIdx.x];
-  TraceEpilogue epi{reinterpret_cast<double *>(values), expo, t};
-  ozaki_tile(smem, scratch + t.a_src, scratch + t.b_src, k_tiles, err, epi);
+  TraceEpilogue epi{reinterpret_cast<double *>(values), expo, tiles};
+  ozaki_tiles(smem, n_tiles, k_tiles, TraceSrc{scratch, tiles}, err, epi);
 }
 
 }  // namespace
@@ -142,8 +152,12 @@ cudaError_t tc_gemm(double2 *out, uint8_t const *scratch, int32_t const *expo,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(kSmemBytes));
   if (e != cudaSuccess) return e;
-  trace_gemm_kernel<<<static_cast<unsigned>(n_tiles), kThreads, kSmemBytes, stream>>>(
-      out, scratch, expo, tiles, k_tiles, err);
+  for (int64_t t0 = 0; t0 < n_tiles; t0 += 0x7fffffffLL) {
+    int64_t const n = n_tiles - t0 < 0x7fffffffLL ? n_tiles - t0 : 0x7fffffffLL;
+    trace_gemm_kernel<<<static_cast<unsigned>(persistent_grid(n)), kThreads, kSmemBytes,
+                        stream>>>(out, scratch, expo, tiles + t0, static_cast<int32_t>(n),
+                                  k_tiles, err);
+  }
   return cudaGetLastError();
 }
 

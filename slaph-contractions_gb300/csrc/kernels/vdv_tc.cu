@@ -10,8 +10,8 @@
 // operator (B) to HBM, already in the tcgen05 core-matrix layout, and streamed
 // into shared memory by the GEMM.  The B columns of all operators of a
 // timeslice form one N dimension (column o nev + j: operator o, eigenvector
-// j), cut into tiles of kTN without padding between operators; grid: m tiles x
-// n tiles x timeslices of a batch.
+// j), cut into tiles of kTN without padding between operators; the tiles of a
+// batch of timeslices (m tiles x n tiles x timeslices) go to persistent CTAs.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -133,6 +133,29 @@ __global__ void phase_fixed_kernel(longlong2 *dst, double2 const *src, int64_t n
   dst[k] = make_longlong2(__double2ll_rn(ldexp(v.x, 62)), __double2ll_rn(ldexp(v.y, 62)));
 }
 
+// Tile i of a launch: m tile i % m_tiles, n tile (i / m_tiles) % n_tiles,
+// batch slot i / (m_tiles n_tiles) (timeslice t0 + slot).  Slot b has its own A
+// slices, B slices and exponents at stride slot_bytes in the scratch buffer:
+// the eigenvectors' exponents, then per operator o >= n_comp (displaced) the
+// exponents of its B columns at (1 + o) nev.
+struct VdvTiles {
+  uint8_t const *scratch;
+  size_t slot_bytes, b_off, e_off;
+  int32_t m_tiles, n_tiles, k_tiles;
+  __device__ __forceinline__ void decode(int i, int &mt, int &nt, int &slot) const {
+    mt = i % m_tiles;
+    nt = (i / m_tiles) % n_tiles;
+    slot = i / (m_tiles * n_tiles);
+  }
+  __device__ __forceinline__ void operator()(int i, uint8_t const *&a, uint8_t const *&b) const {
+    int mt, nt, slot;
+    decode(i, mt, nt, slot);
+    uint8_t const *sbase = scratch + slot * slot_bytes;
+    a = sbase + static_cast<int64_t>(mt) * k_tiles * kStageA;
+    b = sbase + b_off + static_cast<int64_t>(nt) * k_tiles * kStageB;
+  }
+};
+
 // Epilogue of one VdaggerV tile: D = (hi + lo) 2^(e_i + f_c - 14), rows
 // (2i, 2i+1) = (Re, Im) of VdaggerV_o(i, j) for the tile's B columns c = o nev
 // + j, written to operator o's column-major nev x nev block of timeslice t; e:
@@ -140,17 +163,24 @@ __global__ void phase_fixed_kernel(longlong2 *dst, double2 const *src, int64_t n
 // eigenvectors' for momentum operators, |phase| = 1; those of D(V) for the
 // displaced ones, o >= n_comp, at (1 + o) nev).
 struct VdvEpilogue {
+  VdvTiles tl;
   double2 *vdv;
-  int32_t const *expo, *ops;
-  int i0, c0, nev, n_comp, n_cols, Lt, t;
-  __device__ __forceinline__ void operator()(int row, float const (&hi)[kTN],
-                                             float const (&lo)[kTN]) const {
-    int const i = i0 + row / 2;
+  int32_t const *ops;
+  int nev, n_comp, n_cols, Lt, t0;
+  __device__ __forceinline__ void operator()(int it, int row, int col0,
+                                             float const (&hi)[kColsW],
+                                             float const (&lo)[kColsW]) const {
+    int mt, nt, slot;
+    tl.decode(it, mt, nt, slot);
+    int const i = mt * (kTM / 2) + row / 2;
     if (i >= nev) return;
+    int32_t const *expo =
+        reinterpret_cast<int32_t const *>(tl.scratch + slot * tl.slot_bytes + tl.e_off);
+    int const t = t0 + slot;
     int const ei = expo[i];
 #pragma unroll
-    for (int jj = 0; jj < kTN; ++jj) {
-      int const c = c0 + jj;
+    for (int jj = 0; jj < kColsW; ++jj) {
+      int const c = nt * kTN + col0 + jj;
       if (c < n_cols) {
         int const o = c / nev, j = c - o * nev;
         int const ec = o < n_comp ? expo[j] : expo[(1 + o) * nev + j];
@@ -164,25 +194,14 @@ struct VdvEpilogue {
   }
 };
 
-// The GEMM: grid (m_tiles, n_tiles, batch), kThreads threads.  Batch slot b
-// (timeslice t0 + b) has its own A slices, B slices and exponents at stride
-// slot_bytes in the scratch buffer: the eigenvectors' exponents, then per
-// operator o >= n_comp (displaced) the exponents of its B columns at
-// (1 + o) nev.
+// The GEMM: m_tiles x n_tiles x batch tiles over persistent CTAs, kThreads
+// threads each.
 __global__ void __launch_bounds__(kThreads, 1)
-    ozaki_gemm_kernel(uint8_t const *scratch, size_t slot_bytes, size_t b_off, size_t e_off,
-                      double2 *vdv, int32_t const *ops, int32_t n_ops, int32_t n_comp,
-                      int32_t k_tiles, int32_t t0, Geometry g, int *err) {
+    ozaki_gemm_kernel(VdvTiles tl, int32_t n_tiles, double2 *vdv, int32_t const *ops,
+                      int32_t n_ops, int32_t n_comp, int32_t t0, Geometry g, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  int const mt = blockIdx.x, nt = blockIdx.y, slot = blockIdx.z;
-  int const t = t0 + slot;
-  uint8_t const *sbase = scratch + slot * slot_bytes;
-  uint8_t const *a_src = sbase + static_cast<int64_t>(mt) * k_tiles * kStageA;
-  uint8_t const *b_src = sbase + b_off + static_cast<int64_t>(nt) * k_tiles * kStageB;
-  int32_t const *expo = reinterpret_cast<int32_t const *>(sbase + e_off);
-  VdvEpilogue epi{vdv, expo, ops, mt * (kTM / 2), nt * kTN, g.nev, n_comp, n_ops * g.nev,
-                  g.Lt, t};
-  ozaki_tile(smem, a_src, b_src, k_tiles, err, epi);
+  VdvEpilogue epi{tl, vdv, ops, g.nev, n_comp, n_ops * g.nev, g.Lt, t0};
+  ozaki_tiles(smem, n_tiles, tl.k_tiles, tl, err, epi);
 }
 
 }  // namespace
@@ -306,12 +325,12 @@ cudaError_t vdaggerv_tc(double2 *vdv, double2 const *V, longlong2 const *phase_f
       e = cudaEventRecord(gemm_ev[2 * gemm_k], stream);
       if (e != cudaSuccess) return e;
     }
-    ozaki_gemm_kernel<<<dim3(static_cast<unsigned>(L.m_tiles),
-                             static_cast<unsigned>(L.n_tiles), static_cast<unsigned>(nb)),
-                        kThreads, kSmemBytes, stream>>>(base, L.slot_bytes, L.a_bytes, L.e_off,
-                                                        vdv, ops, n, n_comp,
-                                                        static_cast<int32_t>(L.k_tiles), tb, g,
-                                                        err);
+    VdvTiles const tl{base, L.slot_bytes, L.a_bytes, L.e_off, static_cast<int32_t>(L.m_tiles),
+                      static_cast<int32_t>(L.n_tiles), static_cast<int32_t>(L.k_tiles)};
+    int64_t const n_tiles = L.m_tiles * L.n_tiles * nb;
+    ozaki_gemm_kernel<<<static_cast<unsigned>(persistent_grid(n_tiles)), kThreads, kSmemBytes,
+                        stream>>>(tl, static_cast<int32_t>(n_tiles), vdv, ops, n, n_comp, tb, g,
+                                  err);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (timed) {
