@@ -69,6 +69,25 @@ double elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+
+// Row groups of the slicing items [b, e) of one batch: consecutive items of
+// one region with consecutive rows and exponent indices, cut at multiples of
+// `rows` (one 8-row core-matrix group of the operand stream).
+void slice_groups(std::vector<dev::TrSlice> const &it, size_t b, size_t e, int32_t rows,
+                  std::vector<dev::TrSliceGroup> &out) {
+  for (size_t k = b; k < e;) {
+    dev::TrSliceGroup g{};
+    g.dst = it[k].dst;
+    g.row0 = it[k].row;
+    g.expo0 = it[k].expo;
+    do {
+      g.slot[g.n++] = it[k].slot;
+      ++k;
+    } while (k < e && g.n < rows && it[k].dst == g.dst && it[k].row == g.row0 + g.n &&
+             it[k].expo == g.expo0 + g.n && it[k].row % rows != 0);
+    out.push_back(g);
+  }
+}
 }  // namespace
 
 Engine::Engine(slaph_dims const &d) : dims_(d) {
@@ -696,16 +715,22 @@ void Engine::prepare_trace_tc(DeviceSchedule &ds) {
     Wave const &w = s.waves[wi];
     auto &wb = *ds.waves[wi];
     std::vector<dev::TrSlice> av, bv;
+    std::vector<dev::TrSliceGroup> ag, bg;
     std::vector<dev::TrTile> tiles;
     wb.tc_batches.clear();
     DeviceSchedule::TcBatch cur{0, 0, 0, 0, 0, 0};
     size_t used = 0;
     int64_t expo = 0;
     auto close = [&] {
-      cur.n_a = static_cast<int64_t>(av.size()) - cur.a_off;
-      cur.n_b = static_cast<int64_t>(bv.size()) - cur.b_off;
+      // the batch's slicing items as row groups: offsets into ag / bg
+      int64_t const ga = static_cast<int64_t>(ag.size()), gb = static_cast<int64_t>(bg.size());
+      slice_groups(av, static_cast<size_t>(cur.a_off), av.size(), dev::kTrSliceRowsA, ag);
+      slice_groups(bv, static_cast<size_t>(cur.b_off), bv.size(), dev::kTrSliceRowsB, bg);
       cur.n_tiles = static_cast<int64_t>(tiles.size()) - cur.tile_off;
-      if (cur.n_tiles > 0) wb.tc_batches.push_back(cur);
+      if (cur.n_tiles > 0)
+        wb.tc_batches.push_back({ga, static_cast<int64_t>(ag.size()) - ga, gb,
+                                 static_cast<int64_t>(bg.size()) - gb, cur.tile_off,
+                                 cur.n_tiles});
       need = std::max(need, used);
       max_expo = std::max(max_expo, expo);
       cur = {static_cast<int64_t>(av.size()), 0, static_cast<int64_t>(bv.size()), 0,
@@ -773,8 +798,8 @@ void Engine::prepare_trace_tc(DeviceSchedule &ds) {
       }
     }
     close();
-    upload(wb.tc_a, av, stream_);
-    upload(wb.tc_b, bv, stream_);
+    upload(wb.tc_a, ag, stream_);
+    upload(wb.tc_b, bg, stream_);
     upload(wb.tc_tiles, tiles, stream_);
     SLAPH_CK(cudaStreamSynchronize(stream_));
   }
@@ -1400,8 +1425,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
           auto const &b = wb.tc_batches[bi];
           SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi], stream_));
           cuda_check(dev::trace_tc_slice(tc_scratch_.as<uint8_t>(), tr_expo_.as<int32_t>(),
-                                         wb.tc_a.as<dev::TrSlice>() + b.a_off, b.n_a,
-                                         wb.tc_b.as<dev::TrSlice>() + b.b_off, b.n_b,
+                                         wb.tc_a.as<dev::TrSliceGroup>() + b.a_off, b.n_a,
+                                         wb.tc_b.as<dev::TrSliceGroup>() + b.b_off, b.n_b,
                                          df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds,
                                          stream_),
                      "trace_tc_slice");

@@ -46,7 +46,8 @@ struct DeviceSchedule {
   DevBuf q0m, q1r, q2m, q0, q1, q2;
   DevBuf shape_i, shape_j, shape_mask, shape_off;
   // Dense trace groups of a wave cut into batches that fit the tensor-core
-  // scratch buffer: slicing items and GEMM tiles per batch.
+  // scratch buffer: slicing row groups (a_off, n_a / b_off, n_b index tc_a /
+  // tc_b) and GEMM tiles per batch.
   struct TcBatch {
     int64_t a_off, n_a, b_off, n_b, tile_off, n_tiles;
   };

@@ -197,6 +197,20 @@ struct TrSlice {
   int32_t expo;  // index of the matrix's exponent in the exponent array
   int32_t pad;
 };
+// Matrices of one 8-row core-matrix group of a region, sliced together so that
+// every store covers whole core matrices: kTrSliceRowsA consecutive complex
+// rows of an A region (eight rows of A', two per matrix) or kTrSliceRowsB
+// consecutive columns of a B region, from a row that is a multiple of that
+// count; exponent indices expo0, expo0 + 1, ...
+constexpr int32_t kTrSliceRowsA = 4, kTrSliceRowsB = 8;
+struct TrSliceGroup {
+  int64_t dst;    // byte offset of the region in the scratch buffer
+  int32_t row0;   // first row (A) or column (B) of the group
+  int32_t n;      // matrices in the group (1 .. 4 for A, 1 .. 8 for B)
+  int32_t expo0;  // exponent index of the first matrix
+  int32_t slot[8];
+  int32_t pad;
+};
 // One output tile of 64 A groups x 80 B groups of one (group, entry) GEMM.
 struct TrTile {
   int64_t a_src, b_src;  // byte offsets of the tile's A and B operand streams
@@ -211,10 +225,12 @@ int64_t trace_tc_k_tiles(int32_t eds);
 size_t trace_tc_a_bytes(int32_t rows, int32_t eds);  // A region of `rows` matrices
 size_t trace_tc_b_bytes(int32_t cols, int32_t eds);  // B region of `cols` matrices
 // Slices the A matrices (natural layout, conjugated) and B matrices
-// (transposed layout) of a batch into their regions of `scratch`.
-cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSlice const *a_items, int64_t n_a,
-                           TrSlice const *b_items, int64_t n_b, float4 const *slots_n,
-                           float4 const *slots_t, int32_t eds, cudaStream_t stream);
+// (transposed layout) of a batch into their regions of `scratch`, one row
+// group per CTA.
+cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSliceGroup const *a_groups,
+                           int64_t n_a, TrSliceGroup const *b_groups, int64_t n_b,
+                           float4 const *slots_n, float4 const *slots_t, int32_t eds,
+                           cudaStream_t stream);
 // The GEMM tiles of a batch; FP64 trace values into `values`.
 cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
                           TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,

@@ -10,9 +10,9 @@
 // plain product), B columns are the transposed B matrices.
 //
 // Operands are double-float matrices (float4 (re_hi, re_lo, im_hi, im_lo)) in
-// the natural (A) and transposed (B) layouts.  trace_slice_kernel cuts one
-// matrix per CTA into the operand stream of its GEMM region, with the
-// matrix's exponent; trace_gemm_kernel computes 64 x 80 complex output tiles
+// the natural (A) and transposed (B) layouts.  trace_slice_kernel cuts the
+// matrices of one 8-row core-matrix group per CTA into the operand stream of
+// their GEMM region, with each matrix's exponent; trace_gemm_kernel computes 64 x 80 complex output tiles
 // (persistent CTAs, one per SM) and writes FP64 trace values: the 32 lanes of
 // a warp hold 16 consecutive A groups (re, im) of one output column, so the
 // stores of each column are 256 contiguous bytes.
@@ -30,43 +30,86 @@ namespace {
 
 using namespace tc;
 
-constexpr int kSliceThreads = 128;
+constexpr int kSliceThreads = 256;  // eight warps per row group
 
-// One matrix per CTA: exponent of its largest |re|, |im| (from the high
-// words), then its slices.  Integer and FP32 operations only: the fixed-point
-// value of a double-float entry is the sum of those of its two words.
+// One row group per CTA (TrSliceGroup): warp w first takes the exponent of
+// matrix w (its largest |re|, |im|, from the high words), then the warps take
+// k-tiles in turn.  In a k-tile, lane (r, kc) = (lane / 4, lane % 4) converts
+// the four complex entries 4 kc .. 4 kc + 3 of core-matrix row r (B: matrix
+// r; A: matrix r / 2, A' row parity r % 2) into one 16-byte row segment per
+// slice, so that each slice store of a warp writes 512 contiguous bytes.
+// Integer and FP32 operations only: the fixed-point value of a double-float
+// entry is the sum of those of its two words.  Rows past the group's n are not
+// written (the GEMM tiles mask them).
 template <bool kIsA>
 __global__ void __launch_bounds__(kSliceThreads)
-    trace_slice_kernel(uint8_t *scratch, int32_t *expo, TrSlice const *items,
+    trace_slice_kernel(uint8_t *scratch, int32_t *expo, TrSliceGroup const *groups,
                        float4 const *slots, int32_t eds) {
-  TrSlice const it = items[blockIdx.x];
+  TrSliceGroup const gr = groups[blockIdx.x];
   int64_t const ms = static_cast<int64_t>(eds) * eds;
-  int64_t const k_tiles = ms / (kTK / 2);
-  float4 const *src = slots + static_cast<int64_t>(it.slot) * ms;
-  unsigned int mx = 0;
-  for (int64_t m = threadIdx.x; m < ms; m += kSliceThreads) {
-    float4 const v = src[m];
-    mx = max(mx, max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.z) & 0x7FFFFFFFu));
+  int32_t const k_tiles = static_cast<int32_t>(ms / (kTK / 2));
+  int const warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  __shared__ int e_sh[8];
+  if (warp < gr.n) {
+    float4 const *src = slots + static_cast<int64_t>(gr.slot[warp]) * ms;
+    unsigned int mx = 0;
+    for (int64_t m = lane; m < ms; m += 32) {
+      float4 const v = src[m];
+      mx = max(mx, max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.z) & 0x7FFFFFFFu));
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    // |hi + lo| < 2^e whenever |hi| < 2^e (|lo| <= ulp(hi) / 2).
+    int const e = expo_of_absbits(mx);
+    if (lane == 0) {
+      e_sh[warp] = e;
+      expo[gr.expo0 + warp] = e;
+    }
   }
-  mx = __reduce_max_sync(0xffffffffu, mx);
-  __shared__ unsigned int red[kSliceThreads / 32];
-  if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = mx;
   __syncthreads();
-  mx = red[0];
+  int const r = lane / 4, kc = lane % 4;
+  int const mi = kIsA ? r / 2 : r;  // matrix of this lane
+  if (mi >= gr.n) return;
+  int const e = e_sh[mi];
+  float4 const *src = slots + static_cast<int64_t>(gr.slot[mi]) * ms + 4 * kc;
+  uint8_t *region = scratch + gr.dst;
+  uint8_t *base;
+  uint32_t blk;
+  if (kIsA) {
+    int const cr = gr.row0 + mi, arow = 2 * (cr % (kTM / 2)) + (r & 1);
+    base = region + static_cast<int64_t>(cr / (kTM / 2)) * k_tiles * kStageA +
+           ((arow >> 3) * 4 + kc) * 128 + (arow & 7) * 16;
+    blk = kABlk;
+  } else {
+    int const c = gr.row0 + mi, rr = c % kTN;
+    base = region + static_cast<int64_t>(c / kTN) * k_tiles * kStageB +
+           ((rr >> 3) * 4 + kc) * 128 + (rr & 7) * 16;
+    blk = kBBlk;
+  }
+  for (int kt = warp; kt < k_tiles; kt += kSliceThreads / 32) {
+    uint32_t w[kSlices][4];
 #pragma unroll
-  for (int w = 1; w < kSliceThreads / 32; ++w) mx = max(mx, red[w]);
-  // |hi + lo| < 2^e whenever |hi| < 2^e (|lo| <= ulp(hi) / 2).
-  int const e = expo_of_absbits(mx);
-  if (threadIdx.x == 0) expo[it.expo] = e;
-  uint8_t *region = scratch + it.dst;
-  for (int64_t m = threadIdx.x; m < ms; m += kSliceThreads) {
-    float4 const v = src[m];
-    long long const fr = fixed55f(v.x, e) + fixed55f(v.y, e);
-    long long const fi = fixed55f(v.z, e) + fixed55f(v.w, e);
-    if (kIsA)
-      put_a_fx(region, k_tiles, it.row, m, fr, -fi);  // conj: A' rows give sum x_k y_k
-    else
-      put_b_fx(region, k_tiles, it.row, m, fr, fi);
+    for (int q = 0; q < 4; ++q) {
+      float4 const v = src[kt * (kTK / 2) + q];
+      long long const fr = fixed55f(v.x, e) + fixed55f(v.y, e);
+      long long const fi = fixed55f(v.z, e) + fixed55f(v.w, e);
+      float dre[kSlices], dim[kSlices];
+      digits6(fr, dre);
+      if (kIsA) {
+        // conj: A' rows (Re x, Im x) and (-Im x, Re x) of x = conj(v)
+        digits6(-fi, dim);
+#pragma unroll
+        for (int s = 0; s < kSlices; ++s)
+          w[s][q] = (r & 1) ? bf16x2(-dim[s], dre[s]) : bf16x2(dre[s], dim[s]);
+      } else {
+        digits6(fi, dim);
+#pragma unroll
+        for (int s = 0; s < kSlices; ++s) w[s][q] = bf16x2(dre[s], dim[s]);
+      }
+    }
+    uint8_t *dst = base + static_cast<int64_t>(kt) * (kIsA ? kStageA : kStageB);
+#pragma unroll
+    for (int s = 0; s < kSlices; ++s)
+      *reinterpret_cast<uint4 *>(dst + s * blk) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
   }
 }
 
@@ -123,16 +166,17 @@ size_t trace_tc_b_bytes(int32_t cols, int32_t eds) {
   return static_cast<size_t>((cols + kTN - 1) / kTN) * trace_tc_k_tiles(eds) * kStageB;
 }
 
-cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSlice const *a_items, int64_t n_a,
-                           TrSlice const *b_items, int64_t n_b, float4 const *slots_n,
-                           float4 const *slots_t, int32_t eds, cudaStream_t stream) {
+cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSliceGroup const *a_groups,
+                           int64_t n_a, TrSliceGroup const *b_groups, int64_t n_b,
+                           float4 const *slots_n, float4 const *slots_t, int32_t eds,
+                           cudaStream_t stream) {
   if ((static_cast<int64_t>(eds) * eds) % (kTK / 2) != 0) return cudaErrorInvalidValue;
   if (n_a > 0)
     trace_slice_kernel<true><<<static_cast<unsigned>(n_a), kSliceThreads, 0, stream>>>(
-        scratch, expo, a_items, slots_n, eds);
+        scratch, expo, a_groups, slots_n, eds);
   if (n_b > 0)
     trace_slice_kernel<false><<<static_cast<unsigned>(n_b), kSliceThreads, 0, stream>>>(
-        scratch, expo, b_items, slots_t, eds);
+        scratch, expo, b_groups, slots_t, eds);
   return cudaGetLastError();
 }
 
