@@ -2,6 +2,7 @@
 #include "engine.hpp"
 
 #include <algorithm>
+#include <climits>
 #include <array>
 #include <map>
 #include <cstdio>
@@ -808,6 +809,126 @@ void Engine::prepare_trace_tc(DeviceSchedule &ds) {
   ds.tc_ready = true;
 }
 
+// Tensor-core plan of the factor products (product_tc.cu), per wave and
+// dependency level.  Left matrices are taken in order of first appearance; a
+// group starts with the next unused one and adds, up to 64 / eds, the unused
+// left matrix that shares the most right matrices with the group so far
+// (fewest products computed and dropped).  The group's columns are the union
+// of its members' right matrices in index order.
+void Engine::prepare_product_tc(DeviceSchedule &ds) {
+  if (ds.p_ready) return;
+  Schedule const &s = ds.s;
+  int32_t const eds = s.eds;
+  int32_t const per_group = 64 / eds;
+  int64_t const a_bytes = dev::prod_tc_a_bytes(eds), r_bytes = dev::prod_tc_r_bytes(eds);
+  size_t need = 0;
+  int64_t max_expo = 0;
+  for (size_t wi = 0; wi < s.waves.size(); ++wi) {
+    Wave const &w = s.waves[wi];
+    auto &wb = *ds.waves[wi];
+    std::vector<dev::ProdGroup> groups;
+    std::vector<int32_t> r_slots, u_list, out_tab;
+    std::vector<dev::ProdTile> tiles;
+    wb.p_levels.clear();
+    for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
+      int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
+      DeviceSchedule::PLevel pl{static_cast<int64_t>(groups.size()), 0,
+                                static_cast<int64_t>(r_slots.size()), 0,
+                                static_cast<int64_t>(tiles.size()), 0};
+      // left matrices (by first appearance) with their (right index, slot)
+      // lists; right matrices numbered by first appearance
+      std::map<int32_t, int32_t> lidx, ridx;
+      std::vector<int32_t> l_slot;
+      std::vector<std::vector<std::pair<int32_t, int32_t>>> lr;
+      int64_t const r0 = static_cast<int64_t>(r_slots.size());
+      for (int64_t k = b; k < e; ++k) {
+        ProdInst const &pi = w.prods[k];
+        auto li = lidx.emplace(pi.a, static_cast<int32_t>(l_slot.size()));
+        if (li.second) {
+          l_slot.push_back(pi.a);
+          lr.emplace_back();
+        }
+        auto ri = ridx.emplace(pi.b, static_cast<int32_t>(r_slots.size() - r0));
+        if (ri.second) r_slots.push_back(pi.b);
+        lr[li.first->second].push_back({ri.first->second, pi.c});
+      }
+      int32_t const n_l = static_cast<int32_t>(l_slot.size());
+      int32_t const n_r = static_cast<int32_t>(r_slots.size() - r0);
+      std::vector<std::vector<int32_t>> inv(n_r);
+      for (int32_t li = 0; li < n_l; ++li) {
+        std::sort(lr[li].begin(), lr[li].end());
+        for (auto const &rc : lr[li]) inv[rc.first].push_back(li);
+      }
+      std::vector<char> used(n_l, 0);
+      std::vector<int32_t> cnt(n_l, 0), touched;
+      for (int32_t li = 0; li < n_l; ++li) {
+        if (used[li]) continue;
+        std::vector<int32_t> mem{li};
+        used[li] = 1;
+        while (static_cast<int32_t>(mem.size()) < per_group) {
+          touched.clear();
+          for (int32_t m : mem)
+            for (auto const &rc : lr[m])
+              for (int32_t l2 : inv[rc.first])
+                if (!used[l2] && cnt[l2]++ == 0) touched.push_back(l2);
+          int32_t best = -1;
+          for (int32_t l2 : touched)
+            if (best < 0 || cnt[l2] > cnt[best] || (cnt[l2] == cnt[best] && l2 < best)) best = l2;
+          for (int32_t l2 : touched) cnt[l2] = 0;
+          if (best < 0) break;
+          mem.push_back(best);
+          used[best] = 1;
+        }
+        std::vector<int32_t> uni;
+        for (int32_t m : mem)
+          for (auto const &rc : lr[m]) uni.push_back(rc.first);
+        std::sort(uni.begin(), uni.end());
+        uni.erase(std::unique(uni.begin(), uni.end()), uni.end());
+        dev::ProdGroup g{};
+        for (int x = 0; x < 4; ++x) g.l[x] = -1;
+        g.n_l = static_cast<int32_t>(mem.size());
+        for (int32_t x = 0; x < g.n_l; ++x) g.l[x] = l_slot[mem[x]];
+        g.n_u = static_cast<int32_t>(uni.size());
+        g.u_off = static_cast<int32_t>(u_list.size());
+        int32_t const gi = static_cast<int32_t>(groups.size() - pl.g_off);
+        g.ea = 64 * gi;
+        for (int32_t u : uni) {
+          u_list.push_back(u);
+          for (int x = 0; x < 4; ++x) {
+            int32_t slot = -1;
+            if (x < g.n_l) {
+              auto const &v = lr[mem[x]];
+              auto it = std::lower_bound(v.begin(), v.end(), std::make_pair(u, INT32_MIN));
+              if (it != v.end() && it->first == u) slot = it->second;
+            }
+            out_tab.push_back(slot);
+          }
+        }
+        int32_t const n_t = (eds * g.n_u + dev::kTrTileCols - 1) / dev::kTrTileCols;
+        for (int32_t nt = 0; nt < n_t; ++nt) tiles.push_back({gi, nt});
+        groups.push_back(g);
+      }
+      pl.n_g = static_cast<int64_t>(groups.size()) - pl.g_off;
+      pl.n_r = n_r;
+      pl.n_t = static_cast<int64_t>(tiles.size()) - pl.t_off;
+      wb.p_levels.push_back(pl);
+      size_t const r_off = static_cast<size_t>((pl.n_g * a_bytes + 1023) / 1024 * 1024);
+      need = std::max(need, r_off + static_cast<size_t>(n_r) * r_bytes);
+      max_expo = std::max(max_expo, 64 * pl.n_g + static_cast<int64_t>(n_r) * eds);
+    }
+    if (u_list.size() > 0x7fffffffULL) throw UnsupportedError("product GEMM lists above 2^31");
+    upload(wb.p_groups, groups, stream_);
+    upload(wb.p_rslots, r_slots, stream_);
+    upload(wb.p_ulist, u_list, stream_);
+    upload(wb.p_out, out_tab, stream_);
+    upload(wb.p_tiles, tiles, stream_);
+    SLAPH_CK(cudaStreamSynchronize(stream_));
+  }
+  ds.p_scratch = need;
+  ds.p_expo = max_expo;
+  ds.p_ready = true;
+}
+
 // Tensor-core plan of the Q1/Q2 factors (factor_tc.cu).  Per timeslice t:
 //   X1[t]  rows (Q1R r at t, a), columns (r2, b, d, c), K = v:
 //          A = conj(Q1R_r(a, v)), B = P_r2((4t+d) nev + v, b eds + c)
@@ -1376,10 +1497,12 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
     // ---- waves: products, traces, terms, accumulation
     values_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_values));
     term_val_.reserve(sizeof(double2) * std::max<int64_t>(1, s.max_terms));
+    bool const p_tc = mixed && dev::prod_tc_supported(eds);
     if (mixed) {
       prepare_trace_tc(ds);
-      tc_scratch_.reserve(std::max<size_t>(1, ds.tc_scratch));
-      tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, ds.tc_expo));
+      if (p_tc) prepare_product_tc(ds);
+      tc_scratch_.reserve(std::max<size_t>(1, std::max(ds.tc_scratch, ds.p_scratch)));
+      tr_expo_.reserve(sizeof(int32_t) * std::max<int64_t>(1, std::max(ds.tc_expo, ds.p_expo)));
       err_.reserve(sizeof(int));
       SLAPH_CK(cudaMemsetAsync(err_.as<void>(), 0, sizeof(int), stream_));
     }
@@ -1391,11 +1514,24 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
       for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
         int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
         if (e <= b) continue;
-        if (mixed)
+        if (mixed && p_tc) {
+          auto const &pl = wb.p_levels[lv];
+          int64_t const r_off =
+              (pl.n_g * dev::prod_tc_a_bytes(eds) + 1023) / 1024 * 1024;
+          launch(dev::products_tc(df_slots_.as<float4>(), df_slots_t_.as<float4>(),
+                                  tc_scratch_.as<uint8_t>(), r_off, tr_expo_.as<int32_t>(),
+                                  64 * pl.n_g, wb.p_groups.as<dev::ProdGroup>() + pl.g_off,
+                                  pl.n_g, wb.p_rslots.as<int32_t>() + pl.r_off, pl.n_r,
+                                  wb.p_ulist.as<int32_t>(), wb.p_out.as<int32_t>(),
+                                  wb.p_tiles.as<dev::ProdTile>() + pl.t_off, pl.n_t, eds,
+                                  err_.as<int>(), stream_),
+                 "products_tc");
+          launches_ += 2;
+        } else if (mixed) {
           launch(dev::products_df(df_slots_.as<float4>(), df_slots_t_.as<float4>(), prods + b,
                                   e - b, eds, stream_),
                  "products_df");
-        else
+        } else
           launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
       }
       int64_t const n_res = static_cast<int64_t>(w.residual_lists.size());

@@ -51,11 +51,18 @@ struct DeviceSchedule {
   struct TcBatch {
     int64_t a_off, n_a, b_off, n_b, tile_off, n_tiles;
   };
+  // Products of one dependency level on the tensor cores: offsets into the
+  // wave's product-GEMM lists.
+  struct PLevel {
+    int64_t g_off, n_g, r_off, n_r, t_off, n_t;
+  };
   struct WaveBufs {
     DevBuf prods, lists, terms, seg_out, seg_off, idx, unique, residual;
     int64_t n_seg = 0;
     DevBuf tc_a, tc_b, tc_tiles;
     std::vector<TcBatch> tc_batches;
+    DevBuf p_groups, p_rslots, p_ulist, p_out, p_tiles;
+    std::vector<PLevel> p_levels;
   };
   std::vector<std::unique_ptr<WaveBufs>> waves;
   double plan_seconds = 0;
@@ -73,6 +80,10 @@ struct DeviceSchedule {
   size_t f_scratch = 0;
   int64_t f_out = 0, f_expo = 0;  // doubles2 of dense outputs, exponents per batch
   bool tc_ready = false;
+  // Products on the tensor cores: scratch bytes and exponents of the largest level.
+  bool p_ready = false;
+  size_t p_scratch = 0;
+  int64_t p_expo = 0;
   size_t tc_scratch = 0;   // bytes of scratch the batches need
   int64_t tc_expo = 0;     // exponents per batch (maximum)
 };
@@ -160,6 +171,7 @@ class Engine {
   std::unique_ptr<DeviceSchedule> make_schedule(slaph_plan const *plan, int single_block_pair);
   void prepare_trace_tc(DeviceSchedule &ds);
   void prepare_factor_tc(DeviceSchedule &ds);
+  void prepare_product_tc(DeviceSchedule &ds);
   void launch(cudaError_t e, char const *what) {
     cuda_check(e, what);
     ++launches_;

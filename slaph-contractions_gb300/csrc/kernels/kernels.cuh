@@ -182,6 +182,35 @@ cudaError_t factors_df(float4 *sn, float4 *st, float4 *q0m_buf, float4 *q1r_buf,
 // slots[c] = slots[a] * slots[b] in double-float, both layouts written.
 cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int64_t n,
                         int32_t eds, cudaStream_t stream);
+// The same products on the tensor cores (product_tc.cu), for eds = 16, 32 or
+// 64.  The products of one dependency level come in groups of up to 64 / eds
+// left matrices (slots l[0..n_l)) with the union of their right matrices:
+// column block u of group g is right matrix u_list[g.u_off + u] (an index into
+// the level's r_slots) and out_tab[4 (g.u_off + u) + l] is the slot of product
+// l x u, or -1 when the level does not ask for it.  Tiles: (group, n tile of
+// 80 columns).  Scratch: the groups' A regions (prod_tc_a_bytes each) from 0,
+// the right-matrix streams (prod_tc_r_bytes each) from r_off; exponents: 64
+// per group from 0, eds per right matrix from r_expo.
+struct ProdGroup {
+  int32_t l[4];   // left-matrix slots
+  int32_t n_l;    // left matrices in the group (1 .. 64 / eds)
+  int32_t n_u;    // right matrices in the union
+  int32_t u_off;  // first column block in u_list / out_tab
+  int32_t ea;     // exponent index of the group's row 0 (64 g)
+};
+struct ProdTile {
+  int32_t group, nt;
+};
+__host__ __device__ inline int64_t prod_tc_r_bytes(int32_t eds) {
+  return 24LL * eds * eds;  // (eds / 16) k-tiles x 6 slices x eds columns x 32 bytes
+}
+bool prod_tc_supported(int32_t eds);
+int64_t prod_tc_a_bytes(int32_t eds);
+cudaError_t products_tc(float4 *slots_n, float4 *slots_t, uint8_t *scratch, int64_t r_off,
+                        int32_t *expo, int64_t r_expo, ProdGroup const *groups, int64_t n_groups,
+                        int32_t const *r_slots, int64_t n_r, int32_t const *u_list,
+                        int32_t const *out_tab, ProdTile const *tiles, int64_t n_tiles,
+                        int32_t eds, int *err, cudaStream_t stream);
 // Trace values as double-float pairs (re_hi, re_lo, im_hi, im_lo) into
 // values_df, laid out as for traces().
 cudaError_t traces_df(float4 *values_df, TraceList const *lists, int32_t const *which,

@@ -302,9 +302,12 @@ __device__ __forceinline__ int expo_of_max(double m) {
 
 // The tiles of one launch, each a 128 x 80 output tile of D = A' B^T over
 // k_tiles k-tiles, computed by a persistent CTA: CTA b takes tiles b, b + G,
-// b + 2G, ... (G = gridDim.x, at most one CTA per SM).  src(i, a, b) gives the
-// kStageA / kStageB blocks of tile i (consecutive per k-tile).  Must be called
-// by all kThreads threads with kSmemBytes of dynamic shared memory.
+// b + 2G, ... (G = gridDim.x, at most one CTA per SM).  src.load(i, kt, dst,
+// bar, lane), called by all lanes of the producer warp, issues the copies of
+// k-tile kt of tile i into the stage at dst, announcing their bytes on bar
+// (load_contiguous for operands whose kStageA / kStageB blocks are
+// consecutive per k-tile).  Must be called by all kThreads threads with
+// kSmemBytes of dynamic shared memory.
 //
 // Roles: warp kProducerWarp issues the bulk copies, running ahead across tile
 // boundaries; warp kMmaWarp issues tcgen05.mma; promotion warps 0..7 read the
@@ -350,6 +353,16 @@ __device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[N][8]) {
                    "+r"(r[l][5]), "+r"(r[l][6]), "+r"(r[l][7]));
 }
 
+// Stage loader for tiles whose A and B k-tile blocks are contiguous: lane 0
+// copies block kt of a (kStageA bytes) and of b (kStageB bytes).
+__device__ __forceinline__ void load_contiguous(uint8_t const *a, uint8_t const *b, int kt,
+                                                uint8_t *dst, uint64_t *bar, int lane) {
+  if (lane != 0) return;
+  mbar_expect_tx(bar, kStageBytes);
+  bulk_g2s(dst, a + static_cast<int64_t>(kt) * kStageA, kStageA, bar);
+  bulk_g2s(dst + kStageA, b + static_cast<int64_t>(kt) * kStageB, kStageB, bar);
+}
+
 template <typename Src, typename Epilogue>
 __device__ __forceinline__ void ozaki_tiles(uint8_t *smem, int n_tiles, int k_tiles,
                                             Src const &src, int *err, Epilogue const &epi) {
@@ -384,31 +397,26 @@ __device__ __forceinline__ void ozaki_tiles(uint8_t *smem, int n_tiles, int k_ti
   uint32_t const tmem = tmem_slot;
 
   if (warp == kProducerWarp) {
-    if (lane == 0) {
-      int64_t g = 0;  // k-tiles issued over all tiles of this CTA
-      bool ok = true;
-      for (int i = first_tile; i < n_tiles && ok; i += tile_step) {
-        uint8_t const *a_src, *b_src;
-        src(i, a_src, b_src);
-        for (int kt = 0; kt < k_tiles; ++kt, ++g) {
-          int const s = static_cast<int>(g % kStages);
-          uint32_t const use = static_cast<uint32_t>(g / kStages);
-          if (g >= kStages && !mbar_wait(&empty_bar[s], (use - 1) & 1, err, 1)) {
-            ok = false;
-            break;
-          }
-          uint8_t *dst = smem + s * kStageBytes;
-          mbar_expect_tx(&full_bar[s], kStageBytes);
-          bulk_g2s(dst, a_src + static_cast<int64_t>(kt) * kStageA, kStageA, &full_bar[s]);
-          bulk_g2s(dst + kStageA, b_src + static_cast<int64_t>(kt) * kStageB, kStageB,
-                   &full_bar[s]);
+    int64_t g = 0;  // k-tiles issued over all tiles of this CTA
+    bool ok = true;
+    for (int i = first_tile; i < n_tiles && ok; i += tile_step) {
+      for (int kt = 0; kt < k_tiles; ++kt, ++g) {
+        int const s = static_cast<int>(g % kStages);
+        uint32_t const use = static_cast<uint32_t>(g / kStages);
+        bool free_ok = true;
+        if (lane == 0 && g >= kStages) free_ok = mbar_wait(&empty_bar[s], (use - 1) & 1, err, 1);
+        if (!__shfl_sync(0xffffffffu, free_ok, 0)) {
+          ok = false;
+          break;
         }
+        src.load(i, kt, smem + s * kStageBytes, &full_bar[s], lane);
       }
-      // The copies of the last stages have landed before shared memory is
-      // released (immediate when the MMA warp consumed them).
+    }
+    // The copies of the last stages have landed before shared memory is
+    // released (immediate when the MMA warp consumed them).
+    if (lane == 0)
       for (int64_t q = g > kStages ? g - kStages : 0; q < g; ++q)
         mbar_wait(&full_bar[q % kStages], static_cast<uint32_t>(q / kStages) & 1, err, 6);
-    }
   } else if (warp == kMmaWarp) {
     if (lane == 0) {  // MMA issuer
       bool ok = true;

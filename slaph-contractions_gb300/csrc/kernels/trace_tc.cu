@@ -140,9 +140,10 @@ struct TraceEpilogue {
 struct TraceSrc {
   uint8_t const *scratch;
   TrTile const *tiles;
-  __device__ __forceinline__ void operator()(int i, uint8_t const *&a, uint8_t const *&b) const {
-    a = scratch + tiles[i].a_src;
-    b = scratch + tiles[i].b_src;
+  __device__ __forceinline__ void load(int i, int kt, uint8_t *dst, uint64_t *bar,
+                                       int lane) const {
+    if (lane == 0)
+      load_contiguous(scratch + tiles[i].a_src, scratch + tiles[i].b_src, kt, dst, bar, 0);
   }
 };
 

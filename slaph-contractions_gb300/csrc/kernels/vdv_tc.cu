@@ -147,12 +147,15 @@ struct VdvTiles {
     nt = (i / m_tiles) % n_tiles;
     slot = i / (m_tiles * n_tiles);
   }
-  __device__ __forceinline__ void operator()(int i, uint8_t const *&a, uint8_t const *&b) const {
+  __device__ __forceinline__ void load(int i, int kt, uint8_t *dst, uint64_t *bar,
+                                       int lane) const {
+    if (lane != 0) return;
     int mt, nt, slot;
     decode(i, mt, nt, slot);
     uint8_t const *sbase = scratch + slot * slot_bytes;
-    a = sbase + static_cast<int64_t>(mt) * k_tiles * kStageA;
-    b = sbase + b_off + static_cast<int64_t>(nt) * k_tiles * kStageB;
+    load_contiguous(sbase + static_cast<int64_t>(mt) * k_tiles * kStageA,
+                    sbase + b_off + static_cast<int64_t>(nt) * k_tiles * kStageB, kt, dst, bar,
+                    0);
   }
 };
 
