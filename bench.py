@@ -394,7 +394,9 @@ def run_engine(args):
                   "ozaki_gemm_kernel (VdaggerV GEMM)": ktim[11] / K,
                   "vdaggerv stage (slicing + ozaki_gemm_kernel)" if precision == 1
                   else "vdaggerv stage (vdv_fp64_kernel)": stage_ms[0],
-                  "factor stage (q*_kernels, factor GEMMs)": stage_ms[1]}
+                  "factor stage (q*_kernels, factor GEMMs)": stage_ms[1],
+                  "factor products (slicing + product_gemm_kernel)" if precision == 1
+                  else "factor products (product_kernel)": ktim[14] / K}
     # Roofline candidates, one kernel each: (time per step in ms, roofline).
     cands = []
     if precision == 1 and ktim[8] > 0:

@@ -416,8 +416,9 @@ int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
  * out[9] its launch count, out[10] the slicing of its operands, out[11] the
  * split-precision VdaggerV GEMM alone (summed over its launches; set by the
  * build), out[12] its launch count, out[13] the last HYP smearing
- * (slaph_engine_smear_gauge_hyp).  Returns the number of values written
- * (<= n, at most 14). */
+ * (slaph_engine_smear_gauge_hyp), out[14] the factor products (summed over
+ * their dependency levels), out[15] the number of those levels.  Returns the
+ * number of values written (<= n, at most 16). */
 int slaph_engine_timings(const slaph_engine *eng, double *out, int n);
 
 /* VdaggerV of one operator on one timeslice for callers that cannot let a

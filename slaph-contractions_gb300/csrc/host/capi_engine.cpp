@@ -169,7 +169,7 @@ int slaph_engine_timings(const slaph_engine *eng, double *out, int n) {
     slaph::set_last_error("invalid argument");
     return -1;
   }
-  int const m = n < 14 ? n : 14;
+  int const m = n < 16 ? n : 16;
   for (int i = 0; i < m; ++i) out[i] = eng->e->timings[i];
   return m;
 }

@@ -1376,7 +1376,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   int64_t const n_run = std::max<int64_t>(1, n_outputs * dims_.Lt);
   running_.reserve(sizeof(double2) * n_run);
   SLAPH_CK(cudaMemsetAsync(running_.as<void>(), 0, sizeof(double2) * n_run, stream_));
-  double t_f = 0, t_pt = 0, t_as = 0, t_tr = 0, t_sl = 0, t_gm = 0;
+  double t_f = 0, t_pt = 0, t_as = 0, t_tr = 0, t_sl = 0, t_gm = 0, t_pr = 0;
+  int64_t n_pr = 0;
   int64_t n_tr = 0, n_gm = 0;
   double st[8] = {};
   for (DeviceSchedule *dsp : scheds) {
@@ -1599,6 +1600,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
       SLAPH_CK(cudaEventSynchronize(ev_[4]));
       t_pt += elapsed_ms(ev_[2], ev_[3]);
       t_as += elapsed_ms(ev_[3], ev_[4]);
+      t_pr += elapsed_ms(ev_[2], ev_[5]);
+      n_pr += static_cast<int64_t>(w.prod_level_off.size() > 0 ? w.prod_level_off.size() - 1 : 0);
       if (traced) {
         t_tr += elapsed_ms(ev_[5], ev_[6]);
         ++n_tr;
@@ -1638,6 +1641,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   timings[8] = t_gm;
   timings[9] = static_cast<double>(n_gm);
   timings[10] = t_sl;
+  timings[14] = t_pr;
+  timings[15] = static_cast<double>(n_pr);
 
   // ---- output: C[t] = correlator[t][i] / Lt (src/Diagram.cpp:141-143)
   std::vector<double2> host(static_cast<size_t>(n_outputs * dims_.Lt));

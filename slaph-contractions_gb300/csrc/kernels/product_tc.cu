@@ -16,9 +16,9 @@
 // the left matrices (conjugated, so that the conjugating form gives the plain
 // product), one exponent per row; each distinct right matrix of the level is
 // sliced once into a stream of its own, [k-tile][slice][8-column group][512
-// bytes] with one exponent per column, and the producer of the GEMM gathers the
-// 8-column groups of a tile's B stage from those streams with 512-byte bulk
-// copies.
+// bytes] with one exponent per column, and the producer of the GEMM gathers a
+// tile's B stage from those streams with one bulk copy per (slice, right
+// matrix).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -155,9 +155,9 @@ __global__ void __launch_bounds__(kPSliceThreads)
 }
 
 // Stage loader of the product GEMM: the group's A block (lane 0) and the B
-// stage gathered from the right-matrix streams, one 512-byte copy per (slice,
-// 8-column group) spread over the lanes; padding columns of a group's last
-// tile are not copied (the epilogue skips them).
+// stage gathered from the right-matrix streams, one copy per (slice, right
+// matrix) spread over the lanes; padding columns of a group's last tile are not
+// copied (the epilogue skips them).
 struct ProdTiles {
   uint8_t const *scratch;  // A regions from 0, right-matrix streams from r_off
   int64_t a_bytes, r_off;
@@ -165,66 +165,118 @@ struct ProdTiles {
   ProdGroup const *groups;
   int32_t const *u_list;  // right-matrix index of each group column block
   int32_t eds, k_tiles;
-  __device__ __forceinline__ void load(int i, int kt, uint8_t *dst, uint64_t *bar,
-                                       int lane) const {
+  // One tile's copies: the A block, and per lane up to two B copies (one per
+  // (slice, right matrix overlapping the tile): its columns are contiguous
+  // both in its stream and in the stage), addresses of k-tile 0.
+  struct Ctx {
+    uint8_t const *a;
+    uint8_t const *src[2];
+    uint32_t dst[2], bytes[2];
+    uint32_t tx;
+  };
+  __device__ __forceinline__ Ctx context(int i, int lane) const {
     ProdTile const t = tiles[i];
     ProdGroup const gr = groups[t.group];
+    Ctx c;
+    c.a = scratch + t.group * a_bytes;
     int const c0 = t.nt * kTN;
     int const cols = min(kTN, eds * gr.n_u - c0);  // a multiple of 8
-    int const n_cg = cols / 8, r_cg = eds / 8;
+    c.tx = kStageA + static_cast<uint32_t>(kSlices * cols) * 64u;
+    int64_t const r_bytes = prod_tc_r_bytes(eds);
+    int const r_cg = eds / 8, u0 = c0 / eds, n_blk = (c0 + cols - 1) / eds - u0 + 1;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      int const q = lane + 32 * h;
+      c.bytes[h] = 0;
+      c.src[h] = scratch;
+      c.dst[h] = 0;
+      if (q < kSlices * n_blk) {
+        int const s = q / n_blk, u = u0 + q % n_blk;
+        int const cs = max(c0, u * eds), ce = min(c0 + cols, (u + 1) * eds);
+        c.src[h] = scratch + r_off + u_list[gr.u_off + u] * r_bytes +
+                   (static_cast<int64_t>(s) * r_cg + (cs - u * eds) / 8) * 512;
+        c.dst[h] = kStageA + s * kBBlk + ((cs - c0) / 8) * 512;
+        c.bytes[h] = static_cast<uint32_t>(ce - cs) * 64u;
+      }
+    }
+    return c;
+  }
+  __device__ __forceinline__ void load(Ctx const &c, int kt, uint8_t *dst, uint64_t *bar,
+                                       int lane) const {
     if (lane == 0) {
-      mbar_expect_tx(bar, kStageA + static_cast<uint32_t>(kSlices * n_cg) * 512u);
-      bulk_g2s(dst, scratch + t.group * a_bytes + static_cast<int64_t>(kt) * kStageA, kStageA,
-               bar);
+      mbar_expect_tx(bar, c.tx);
+      bulk_g2s(dst, c.a + static_cast<int64_t>(kt) * kStageA, kStageA, bar);
     }
     __syncwarp();
-    int64_t const r_bytes = prod_tc_r_bytes(eds);
-    for (int q = lane; q < kSlices * n_cg; q += 32) {
-      int const s = q / n_cg, cg = q % n_cg;
-      int const c = c0 + 8 * cg;
-      int const u = c / eds, sub = (c % eds) / 8;
-      uint8_t const *src = scratch + r_off + u_list[gr.u_off + u] * r_bytes +
-                           ((static_cast<int64_t>(kt) * kSlices + s) * r_cg + sub) * 512;
-      bulk_g2s(dst + kStageA + s * kBBlk + cg * 512, src, 512, bar);
-    }
+    // k-tile step of a stream: kSlices x eds columns x 64 bytes
+    int64_t const kt_off = static_cast<int64_t>(kt) * kSlices * eds * 64;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      if (c.bytes[h]) bulk_g2s(dst + c.dst[h], c.src[h] + kt_off, c.bytes[h], bar);
   }
 };
 
+// x 2^sh for |sh| <= 252, as two multiplications by powers of two (each exact
+// for a normal result).
+__device__ __forceinline__ float scale2(float x, int sh) {
+  int const s1 = sh / 2, s2 = sh - s1;
+  return (x * __int_as_float((s1 + 127) << 23)) * __int_as_float((s2 + 127) << 23);
+}
+
 // Epilogue: A' row 2 cr + (re | im), cr = l eds + i; column c = u eds + j.
-// The even lane of each pair holds Re, the odd one Im; after one exchange the
-// even lane writes the natural layout and the odd lane the transposed one.
+// A warp's 32 rows lie in one left matrix l.  Before the tile is promoted,
+// lane k fetches the product slot and the column exponent of the warp's
+// columns k and 32 + k; the column loop takes them by warp shuffles.
+// The even lane of each row pair holds Re, the odd one Im; after one exchange
+// the even lane writes the natural layout and the odd lane the transposed one.
 struct ProdEpilogue {
   ProdTiles tl;
   int32_t const *expo;    // A rows from 0 (64 per group), right columns from r_expo
   int64_t r_expo;
   int32_t const *out_tab;  // [group column block][4]: product slot per left matrix
   float4 *slots_n, *slots_t;
-  __device__ __forceinline__ void operator()(int it, int row, int col0, float const (&hi)[kColsW],
-                                             float const (&lo)[kColsW]) const {
+  struct Pre {
+    int ok, er, cbase;
+    int slot0, ec0, slot1, ec1;
+  };
+  __device__ __forceinline__ Pre prepare(int it, int row, int col0) const {
+    Pre p{0, 0, 0, -1, 0, -1, 0};
     ProdTile const t = tl.tiles[it];
     ProdGroup const gr = tl.groups[t.group];
+    int const eds = tl.eds, lane = threadIdx.x % 32;
+    int const cr = row / 2, l = cr / eds;
+    p.cbase = t.nt * kTN + col0;
+    if (l >= gr.n_l) return p;  // warp-uniform
+    p.ok = 1;
+    p.er = expo[gr.ea + cr];
+    int const ncols = eds * gr.n_u;
+    auto meta = [&](int c, int &slot, int &ec) {
+      if (c >= ncols) return;
+      int const u = c / eds;
+      slot = out_tab[4 * (gr.u_off + u) + l];
+      ec = expo[r_expo + static_cast<int64_t>(tl.u_list[gr.u_off + u]) * eds + c % eds];
+    };
+    meta(p.cbase + lane, p.slot0, p.ec0);
+    if (lane < kColsW - 32) meta(p.cbase + 32 + lane, p.slot1, p.ec1);
+    return p;
+  }
+  __device__ __forceinline__ void operator()(Pre const &p, int, int row, int,
+                                             float const (&hi)[kColsW],
+                                             float const (&lo)[kColsW]) const {
+    if (!p.ok) return;  // warp-uniform
     int const eds = tl.eds;
     int64_t const ms = static_cast<int64_t>(eds) * eds;
-    int const cr = row / 2, l = cr / eds, i = cr % eds;
-    bool const row_ok = l < gr.n_l;
-    int const er = row_ok ? expo[gr.ea + cr] : 0;
-    int const ncols = eds * gr.n_u;
+    int const i = (row / 2) % eds;
 #pragma unroll
     for (int cc = 0; cc < kColsW; ++cc) {
-      int const c = t.nt * kTN + col0 + cc;
-      int slot = -1, ec = 0;
-      if (row_ok && c < ncols) {
-        int const u = c / eds;
-        slot = out_tab[4 * (gr.u_off + u) + l];
-        if (slot >= 0) ec = expo[r_expo + static_cast<int64_t>(tl.u_list[gr.u_off + u]) * eds + c % eds];
-      }
-      int const sh = er + ec - 14;
-      float const h = slot >= 0 ? ldexpf(hi[cc], sh) : 0.f;
-      float const lw = slot >= 0 ? ldexpf(lo[cc], sh) : 0.f;
+      int const slot = __shfl_sync(0xffffffffu, cc < 32 ? p.slot0 : p.slot1, cc % 32);
+      int const ec = __shfl_sync(0xffffffffu, cc < 32 ? p.ec0 : p.ec1, cc % 32);
+      int const sh = max(p.er + ec - 14, -252);
+      float const h = scale2(hi[cc], sh), lw = scale2(lo[cc], sh);
       float const oh = __shfl_xor_sync(0xffffffffu, h, 1);
       float const ol = __shfl_xor_sync(0xffffffffu, lw, 1);
       if (slot < 0) continue;
-      int const j = c % eds;
+      int const j = (p.cbase + cc) % eds;
       if ((row & 1) == 0)
         slots_n[slot * ms + i + static_cast<int64_t>(eds) * j] = make_float4(h, lw, oh, ol);
       else

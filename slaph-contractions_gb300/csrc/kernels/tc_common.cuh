@@ -302,12 +302,15 @@ __device__ __forceinline__ int expo_of_max(double m) {
 
 // The tiles of one launch, each a 128 x 80 output tile of D = A' B^T over
 // k_tiles k-tiles, computed by a persistent CTA: CTA b takes tiles b, b + G,
-// b + 2G, ... (G = gridDim.x, at most one CTA per SM).  src.load(i, kt, dst,
-// bar, lane), called by all lanes of the producer warp, issues the copies of
-// k-tile kt of tile i into the stage at dst, announcing their bytes on bar
-// (load_contiguous for operands whose kStageA / kStageB blocks are
-// consecutive per k-tile).  Must be called by all kThreads threads with
-// kSmemBytes of dynamic shared memory.
+// b + 2G, ... (G = gridDim.x, at most one CTA per SM).  The operands:
+// src.context(i, lane) fetches what the copies of tile i need (called one tile
+// ahead by the producer warp), src.load(ctx, kt, dst, bar, lane), called by all
+// lanes of the producer warp, issues the copies of k-tile kt into the stage at
+// dst and announces their bytes on bar (load_contiguous for operands whose
+// kStageA / kStageB blocks are consecutive per k-tile).  The results:
+// epi.prepare(i, row, col0) fetches the epilogue's data of tile i before its
+// first chunk is promoted, epi(pre, i, row, col0, hi, lo) writes them.  Must be
+// called by all kThreads threads with kSmemBytes of dynamic shared memory.
 //
 // Roles: warp kProducerWarp issues the bulk copies, running ahead across tile
 // boundaries; warp kMmaWarp issues tcgen05.mma; promotion warps 0..7 read the
@@ -315,9 +318,9 @@ __device__ __forceinline__ int expo_of_max(double m) {
 // quadrant w % 4 (rows 32 (w % 4) + lane) and the kColsW columns from
 // kColsW (w / 4) on.  Once the last chunk of a tile is promoted the
 // accumulators are released, so the MMAs of the next tile run while the
-// promotion warps hand the previous tile to the epilogue: epi(i, row, col0,
-// hi, lo) with the double-float (hi, lo) of the row's kColsW columns; the
-// result is (hi + lo) 2^(e_row + e_col - 14).
+// promotion warps hand the previous tile to the epilogue, with the
+// double-float (hi, lo) of the row's kColsW columns; the result is
+// (hi + lo) 2^(e_row + e_col - 14).
 //
 // Chunk value of one column, sum_l E_l 2^-8l: levels 0 and 1 are exact
 // integers in FP32; levels 3..5 (at most 2^-24 of the row scale) are summed in
@@ -399,7 +402,10 @@ __device__ __forceinline__ void ozaki_tiles(uint8_t *smem, int n_tiles, int k_ti
   if (warp == kProducerWarp) {
     int64_t g = 0;  // k-tiles issued over all tiles of this CTA
     bool ok = true;
+    // per-tile operand addresses, fetched one tile ahead
+    auto cur = src.context(first_tile < n_tiles ? first_tile : 0, lane);
     for (int i = first_tile; i < n_tiles && ok; i += tile_step) {
+      auto const nxt = src.context(i + tile_step < n_tiles ? i + tile_step : i, lane);
       for (int kt = 0; kt < k_tiles; ++kt, ++g) {
         int const s = static_cast<int>(g % kStages);
         uint32_t const use = static_cast<uint32_t>(g / kStages);
@@ -409,8 +415,9 @@ __device__ __forceinline__ void ozaki_tiles(uint8_t *smem, int n_tiles, int k_ti
           ok = false;
           break;
         }
-        src.load(i, kt, smem + s * kStageBytes, &full_bar[s], lane);
+        src.load(cur, kt, smem + s * kStageBytes, &full_bar[s], lane);
       }
+      cur = nxt;
     }
     // The copies of the last stages have landed before shared memory is
     // released (immediate when the MMA warp consumed them).
@@ -480,6 +487,8 @@ __device__ __forceinline__ void ozaki_tiles(uint8_t *smem, int n_tiles, int k_ti
     int64_t c_all = 0;
     bool ok = true;
     for (int i = first_tile; i < n_tiles && ok; i += tile_step) {
+      // the tile's epilogue data, loaded while its first chunk is multiplied
+      auto const pre = epi.prepare(i, row, col0);
       float hi[kColsW], lo[kColsW];
 #pragma unroll
       for (int j = 0; j < kColsW; ++j) hi[j] = lo[j] = 0.f;
@@ -536,7 +545,7 @@ __device__ __forceinline__ void ozaki_tiles(uint8_t *smem, int n_tiles, int k_ti
         mbar_arrive(&acc_empty);
       }
       // After a timeout the values are incomplete; *err makes the host discard them.
-      if (ok) epi(i, row, col0, hi, lo);
+      if (ok) epi(pre, i, row, col0, hi, lo);
     }
   }
   tc_fence_before();

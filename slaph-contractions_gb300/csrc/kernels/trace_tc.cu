@@ -119,20 +119,35 @@ struct TraceEpilogue {
   double *values;
   int32_t const *expo;
   TrTile const *tiles;
-  __device__ __forceinline__ void operator()(int i, int row, int col0, float const (&hi)[kColsW],
+  // Lane k holds the exponents of the warp's columns k and 32 + k; the column
+  // loop takes them by warp shuffles.
+  struct Pre {
+    TrTile t;
+    int e0, e1, er;
+  };
+  __device__ __forceinline__ Pre prepare(int i, int row, int col0) const {
+    Pre p;
+    p.t = tiles[i];
+    int const lane = threadIdx.x % 32;
+    p.e0 = col0 + lane < p.t.cols ? expo[p.t.eb + col0 + lane] : 0;
+    p.e1 = lane < kColsW - 32 && col0 + 32 + lane < p.t.cols ? expo[p.t.eb + col0 + 32 + lane] : 0;
+    p.er = row / 2 < p.t.rows ? expo[p.t.ea + row / 2] : 0;
+    return p;
+  }
+  __device__ __forceinline__ void operator()(Pre const &p, int i, int row, int col0,
+                                             float const (&hi)[kColsW],
                                              float const (&lo)[kColsW]) const {
-    TrTile const t = tiles[i];
+    TrTile const &t = p.t;
     int const r = row / 2;
-    if (r >= t.rows) return;
-    int const er = expo[t.ea + r];
+    bool const row_ok = r < t.rows;
     double *dst = values + 2 * (t.out + r) + (row & 1);
 #pragma unroll
     for (int c = 0; c < kColsW; ++c) {
+      int const ec = __shfl_sync(0xffffffffu, c < 32 ? p.e0 : p.e1, c % 32);
       int const col = col0 + c;
-      if (col < t.cols)
+      if (row_ok && col < t.cols)
         dst[2 * static_cast<int64_t>(col) * t.ld] =
-            ldexp(static_cast<double>(hi[c]) + static_cast<double>(lo[c]),
-                  er + expo[t.eb + col] - 14);
+            ldexp(static_cast<double>(hi[c]) + static_cast<double>(lo[c]), p.er + ec - 14);
     }
   }
 };
@@ -140,10 +155,15 @@ struct TraceEpilogue {
 struct TraceSrc {
   uint8_t const *scratch;
   TrTile const *tiles;
-  __device__ __forceinline__ void load(int i, int kt, uint8_t *dst, uint64_t *bar,
+  struct Ctx {
+    uint8_t const *a, *b;
+  };
+  __device__ __forceinline__ Ctx context(int i, int lane) const {
+    return Ctx{scratch + tiles[i].a_src, scratch + tiles[i].b_src};
+  }
+  __device__ __forceinline__ void load(Ctx const &c, int kt, uint8_t *dst, uint64_t *bar,
                                        int lane) const {
-    if (lane == 0)
-      load_contiguous(scratch + tiles[i].a_src, scratch + tiles[i].b_src, kt, dst, bar, 0);
+    if (lane == 0) load_contiguous(c.a, c.b, kt, dst, bar, 0);
   }
 };
 

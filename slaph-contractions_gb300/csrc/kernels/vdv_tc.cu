@@ -147,15 +147,19 @@ struct VdvTiles {
     nt = (i / m_tiles) % n_tiles;
     slot = i / (m_tiles * n_tiles);
   }
-  __device__ __forceinline__ void load(int i, int kt, uint8_t *dst, uint64_t *bar,
-                                       int lane) const {
-    if (lane != 0) return;
+  struct Ctx {
+    uint8_t const *a, *b;
+  };
+  __device__ __forceinline__ Ctx context(int i, int lane) const {
     int mt, nt, slot;
     decode(i, mt, nt, slot);
     uint8_t const *sbase = scratch + slot * slot_bytes;
-    load_contiguous(sbase + static_cast<int64_t>(mt) * k_tiles * kStageA,
-                    sbase + b_off + static_cast<int64_t>(nt) * k_tiles * kStageB, kt, dst, bar,
-                    0);
+    return Ctx{sbase + static_cast<int64_t>(mt) * k_tiles * kStageA,
+               sbase + b_off + static_cast<int64_t>(nt) * k_tiles * kStageB};
+  }
+  __device__ __forceinline__ void load(Ctx const &c, int kt, uint8_t *dst, uint64_t *bar,
+                                       int lane) const {
+    if (lane == 0) load_contiguous(c.a, c.b, kt, dst, bar, 0);
   }
 };
 
@@ -170,7 +174,9 @@ struct VdvEpilogue {
   double2 *vdv;
   int32_t const *ops;
   int nev, n_comp, n_cols, Lt, t0;
-  __device__ __forceinline__ void operator()(int it, int row, int col0,
+  struct Pre {};
+  __device__ __forceinline__ Pre prepare(int, int, int) const { return Pre{}; }
+  __device__ __forceinline__ void operator()(Pre const &, int it, int row, int col0,
                                              float const (&hi)[kColsW],
                                              float const (&lo)[kColsW]) const {
     int mt, nt, slot;

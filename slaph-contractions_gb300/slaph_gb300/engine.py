@@ -182,9 +182,9 @@ class Engine:
         """ms: VdaggerV, factors, products+traces, assembly, planning; launches;
         per-entry trace kernel (ms, launches); trace GEMM (ms, launches);
         operand slicing of the trace GEMM (ms); VdaggerV GEMM (ms, launches);
-        HYP smearing (ms)."""
-        out = np.zeros(14)
-        L.lib().slaph_engine_timings(self._h, L.dptr(out), 14)
+        HYP smearing (ms); factor products (ms, dependency levels)."""
+        out = np.zeros(16)
+        L.lib().slaph_engine_timings(self._h, L.dptr(out), 16)
         return out
 
     def stats(self):
