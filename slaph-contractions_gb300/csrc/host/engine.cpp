@@ -50,8 +50,11 @@ void DevBuf::release() {
 
 namespace {
 
-// Upper bound of the split-precision VdaggerV scratch (timeslice batches).
+// Bounds of the split-precision VdaggerV scratch (timeslice batches): at
+// least kTcScratchCap, up to a third of the free device memory and at most
+// kTcScratchMax (larger batches leave less of the last round of tiles idle).
 constexpr size_t kTcScratchCap = 24ULL << 30;
+constexpr size_t kTcScratchMax = 64ULL << 30;
 // Smallest batch capacity of the tensor-core traces (the VdaggerV scratch is
 // reused when it is larger).
 constexpr size_t kTraceScratchMin = 1ULL << 30;
@@ -377,7 +380,11 @@ void Engine::vdaggerv_build(int precision) {
   if (precision == SLAPH_MIXED) {
     int sms = 0;
     SLAPH_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
-    int32_t const batch = dev::vdaggerv_tc_batch(geo_, std::max(n_all, 1), sms, kTcScratchCap);
+    size_t free_b = 0, total_b = 0;
+    SLAPH_CK(cudaMemGetInfo(&free_b, &total_b));
+    size_t const cap = std::max(kTcScratchCap, std::min(kTcScratchMax, free_b / 3));
+    int32_t const n_t = ring_slots_ > 0 ? std::max(1, ring_slots_ / 2) : dims_.Lt;
+    int32_t const batch = dev::vdaggerv_tc_batch(geo_, std::max(n_all, 1), sms, cap, n_t);
     tc_scratch_.reserve(dev::vdaggerv_tc_scratch_bytes(geo_, std::max(n_all, 1), batch));
     // The scratch may be larger than this batch needs (kept from an earlier
     // call): the launch count follows from what it holds.

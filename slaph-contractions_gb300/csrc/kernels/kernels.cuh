@@ -90,14 +90,18 @@ cudaError_t vdaggerv_fp64(double2 *vdv, double2 const *V, double2 const *phase,
 // Split-BF16 tensor-core VdaggerV (vdv_tc.cu): same result as vdaggerv_fp64
 // to ~1e-13 relative.  scratch: device buffer of at least
 // vdaggerv_tc_scratch_bytes(g, n, batch) bytes, where batch timeslices are
-// processed per launch (vdaggerv_tc_batch picks it from the SM count and a
-// memory cap); err: device int, set non-zero when a bounded wait gave up.
+// processed per launch (vdaggerv_tc_batch picks it from the SM count, the
+// timeslice count and a memory cap); err: device int, set non-zero when a bounded wait gave up.
 size_t vdaggerv_tc_scratch_bytes(Geometry g, int32_t n_ops, int32_t batch);
 // phase_fx[k] = round(phase[k] 2^62) per component, the fixed-point phases the
 // split-precision VdaggerV multiplies with integer arithmetic.
 cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
                         cudaStream_t stream);
-int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes);
+// Timeslices per GEMM launch for n_t timeslices: at most what max_bytes of
+// scratch holds, chosen for the fewest rounds of one tile per SM over all
+// launches (the last round of each launch is the partly idle one).
+int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes,
+                          int32_t n_t);
 // Displaced operators of the split-precision VdaggerV: ops[n_comp + d] is
 // V_t^H D_d(V_t), D_d the displacement steps of operator d applied in place to
 // a copy W of V_t (displace above), momentum not applied.

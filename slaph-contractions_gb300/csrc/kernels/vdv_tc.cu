@@ -239,14 +239,29 @@ size_t vdaggerv_tc_scratch_bytes(Geometry g, int32_t n_ops, int32_t batch) {
   return tc_layout(g, n_ops).slot_bytes * static_cast<size_t>(batch > 0 ? batch : 1);
 }
 
-int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes) {
+int32_t vdaggerv_tc_batch(Geometry g, int32_t n_ops, int32_t sm_count, size_t max_bytes,
+                          int32_t n_t) {
   TcLayout const L = tc_layout(g, n_ops);
-  int64_t const ctas = L.m_tiles * L.n_tiles;
-  int64_t want = (2LL * sm_count + ctas - 1) / ctas;  // at least two waves
-  if (want > g.Lt) want = g.Lt;
-  int64_t const fit = static_cast<int64_t>(max_bytes / L.slot_bytes);
-  if (want > fit) want = fit;
-  return static_cast<int32_t>(want < 1 ? 1 : want);
+  int64_t const per_t = L.m_tiles * L.n_tiles;  // tiles of one timeslice
+  int64_t const sms = sm_count > 0 ? sm_count : 1;
+  int64_t const nt = n_t > 0 ? n_t : 1;
+  int64_t fit = static_cast<int64_t>(max_bytes / L.slot_bytes);
+  if (fit > nt) fit = nt;
+  if (fit < 1) fit = 1;
+  // Persistent CTAs take the tiles of a launch in rounds of one tile per SM;
+  // the batch with the fewest rounds over all nt timeslices wastes the least
+  // of the last round of each launch (the smaller batch on a tie).
+  int64_t best = 1, best_rounds = -1;
+  for (int64_t b = 1; b <= fit; ++b) {
+    int64_t const launches = (nt + b - 1) / b, last = nt - (launches - 1) * b;
+    int64_t const rounds = (launches - 1) * ((per_t * b + sms - 1) / sms) +
+                           (per_t * last + sms - 1) / sms;
+    if (best_rounds < 0 || rounds < best_rounds) {
+      best = b;
+      best_rounds = rounds;
+    }
+  }
+  return static_cast<int32_t>(best);
 }
 
 cudaError_t phase_fixed(longlong2 *phase_fx, double2 const *phase, int64_t n,
