@@ -39,16 +39,15 @@ for p in (str(REPO), str(REPO / "slaph-contractions_gb300")):
 METRIC = "s/gauge-config, VdaggerV+pipi contractions 32³×64: FP64 vs split-prec @1e-10"
 UNIT = "s/gauge-config"
 
-# DRAM bytes (read + write) of the tensor-core kernels per unit of work, from
-# ncu captures of dram__bytes_read.sum + dram__bytes_write.sum on the small
-# 16^3x32 Nev=64 pipi case (one kernel, a few launches, a few GB on the device),
-# scaled to a full launch by the units it processes; the capture and its
-# scaling are in the profile summaries named here.  Empty: no capture yet, the
-# roofline's traffic is then null.
-NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY = {}  # keyed by dilE, per dense-group entry
-NCU_TRACE_GEMM_TRAFFIC_SOURCE = "profiles/trace_gemm_kernel_prof_16x32_pipi.md"
-NCU_VDV_GEMM_DRAM_BYTES_PER_UNIT = {}  # keyed by workload, per (operator, timeslice)
-NCU_VDV_GEMM_TRAFFIC_SOURCE = "profiles/ozaki_gemm_kernel_prof_16x32_pipi.md"
+# DRAM bytes (read + write) of the tensor-core GEMMs per unit of work, from
+# one-pass ncu captures (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# full-size 32^3x64 launches; the captures and the derivation are in the
+# profile summary named here.  Other workloads have no capture: their
+# roofline's traffic is null.
+NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY = {"cfg3_32x64_pipi": 470.0}  # per dense-group entry
+NCU_TRACE_GEMM_TRAFFIC_SOURCE = "profiles/gemm_dram_traffic_cfg3_32x64_pipi.md"
+NCU_VDV_GEMM_DRAM_BYTES_PER_UNIT = {"cfg3_32x64_pipi": 0.867e9}  # per (operator, timeslice)
+NCU_VDV_GEMM_TRAFFIC_SOURCE = "profiles/gemm_dram_traffic_cfg3_32x64_pipi.md"
 
 
 def per_correlator_rel_err(out, ref):
@@ -410,7 +409,7 @@ def run_engine(args):
             "unit": "TFLOP/s", "peak_source": f"{peak_src} ({note})",
             "launches_per_step": n_l, "launch_ms_avg": ktim[8] / K / n_l,
             "algorithmic_per_launch": flops / n_l,
-            "traffic": (NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY.get(w.dilE, 0) * stats[7] / n_l)
+            "traffic": (NCU_TRACE_GEMM_DRAM_BYTES_PER_ENTRY.get(args.workload, 0) * stats[7] / n_l)
             or None,
             "traffic_source": NCU_TRACE_GEMM_TRAFFIC_SOURCE,
             "fp64_equivalent_tflops": 8.0 * eds * eds * stats[7] / (ktim[8] / K / 1e3) / 1e12,

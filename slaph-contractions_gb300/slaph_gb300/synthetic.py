@@ -220,6 +220,8 @@ def grouped_pipi(name, nev, dilE, seed):
 
 CONFIGS["pipi_groups_e4"] = grouped_pipi("pipi_groups_e4", nev=16, dilE=4, seed=606)
 CONFIGS["pipi_groups_e8"] = grouped_pipi("pipi_groups_e8", nev=32, dilE=8, seed=707)
+# 4 dilE = 64: one left matrix per product tile, four k-tiles per product
+CONFIGS["pipi_groups_e16"] = grouped_pipi("pipi_groups_e16", nev=32, dilE=16, seed=808)
 
 
 # 48^3 x 96, Nev 220 (eigenvectors 112 GB, streamed per timeslice): the pipi

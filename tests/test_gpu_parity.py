@@ -195,7 +195,7 @@ def test_vdaggerv_mixed_matches_fp64_and_contract(name, oracle_lib):
     assert e < REL_MIXED_CORR
 
 
-@pytest.mark.parametrize("name", ["pipi_groups_e4", "pipi_groups_e8"])
+@pytest.mark.parametrize("name", ["pipi_groups_e4", "pipi_groups_e8", "pipi_groups_e16"])
 def test_dense_trace_groups_match_oracle(name, oracle_lib):
     """Trace lists forming dense groups: tensor-core GEMMs in the mixed mode,
     the per-entry kernel in FP64; the residual lists take the per-entry
