@@ -48,6 +48,27 @@ void DevBuf::release() {
   n_ = 0;
 }
 
+void HostBuf::reserve(size_t bytes) {
+  if (bytes <= n_) return;
+  release();
+  SLAPH_CK(cudaHostAlloc(&p_, bytes, cudaHostAllocPortable));
+  n_ = bytes;
+}
+
+void HostBuf::release() {
+  if (p_) cudaFreeHost(p_);
+  p_ = nullptr;
+  n_ = 0;
+}
+
+int Engine::read_err_flag() {
+  host_rb_.reserve(sizeof(int));
+  SLAPH_CK(cudaMemcpyAsync(host_rb_.as<int>(), err_.as<void>(), sizeof(int),
+                           cudaMemcpyDeviceToHost, stream_));
+  SLAPH_CK(cudaStreamSynchronize(stream_));
+  return *host_rb_.as<int>();
+}
+
 namespace {
 
 // Bounds of the split-precision VdaggerV scratch (timeslice batches): at
@@ -517,8 +538,7 @@ void Engine::vdaggerv_build(int precision) {
   timings[11] = t_gemm;
   timings[12] = static_cast<double>(n_gemm);
   if (precision == SLAPH_MIXED) {
-    int code = 0;
-    SLAPH_CK(cudaMemcpy(&code, err_.as<void>(), sizeof(int), cudaMemcpyDeviceToHost));
+    int const code = read_err_flag();
     if (code != 0)
       throw TimeoutError("split-precision VdaggerV: a bounded device wait gave up (stage " +
                          std::to_string(code) + ")");
@@ -1621,8 +1641,7 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
         }
     }
     if (mixed) {
-      int code = 0;
-      SLAPH_CK(cudaMemcpy(&code, err_.as<void>(), sizeof(int), cudaMemcpyDeviceToHost));
+      int const code = read_err_flag();
       if (code != 0)
         throw TimeoutError("tensor-core factors or traces: a bounded device wait gave up "
                            "(stage " + std::to_string(code) + ")");
@@ -1652,13 +1671,15 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
   timings[15] = static_cast<double>(n_pr);
 
   // ---- output: C[t] = correlator[t][i] / Lt (src/Diagram.cpp:141-143)
-  std::vector<double2> host(static_cast<size_t>(n_outputs * dims_.Lt));
-  if (!host.empty())
-    SLAPH_CK(cudaMemcpyAsync(host.data(), running_.as<double2>(), host.size() * sizeof(double2),
-                             cudaMemcpyDeviceToHost, stream_));
+  size_t const n_host = static_cast<size_t>(n_outputs * dims_.Lt);
+  host_rb_.reserve(std::max<size_t>(1, n_host) * sizeof(double2));
+  double2 const *host = host_rb_.as<double2>();
+  if (n_host > 0)
+    SLAPH_CK(cudaMemcpyAsync(host_rb_.as<double2>(), running_.as<double2>(),
+                             n_host * sizeof(double2), cudaMemcpyDeviceToHost, stream_));
   SLAPH_CK(cudaStreamSynchronize(stream_));
   double const inv = static_cast<double>(dims_.Lt);
-  for (size_t i = 0; i < host.size(); ++i) {
+  for (size_t i = 0; i < n_host; ++i) {
     corr_out[2 * i] = host[i].x / inv;
     corr_out[2 * i + 1] = host[i].y / inv;
   }

@@ -40,6 +40,28 @@ class DevBuf {
   size_t n_ = 0;
 };
 
+// Page-locked host memory for the engine's read-backs (error flags,
+// correlators): a device-to-host copy into it goes straight to the
+// device-to-host copy engine, instead of waiting behind the host-to-device
+// uploads that pageable copies share their staging with.
+class HostBuf {
+ public:
+  HostBuf() = default;
+  ~HostBuf() { release(); }
+  HostBuf(HostBuf const &) = delete;
+  HostBuf &operator=(HostBuf const &) = delete;
+  void reserve(size_t bytes);  // grows, never shrinks; contents undefined
+  void release();
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(p_);
+  }
+
+ private:
+  void *p_ = nullptr;
+  size_t n_ = 0;
+};
+
 // A schedule plus its work lists resident on the device.
 struct DeviceSchedule {
   Schedule s;
@@ -140,6 +162,8 @@ class Engine {
   std::vector<cudaEvent_t> vdv_ev_;  // two per split-precision VdaggerV GEMM launch
 
   DevBuf V_, peram_, noise_, phase_, phase_fx_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
+  HostBuf host_rb_;  // read-back staging
+  int read_err_flag();  // the device error flag, through host_rb_ on the engine stream
   std::vector<slaph_vdv_op> ops_;
   DevBuf U_, W_, disp_ops_;  // gauge links, displaced eigenvector scratch, displaced op ids
   DevBuf hyp_dec_;           // decorated links of a chunk of timeslices (HYP smearing)
