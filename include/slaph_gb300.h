@@ -402,7 +402,10 @@ int64_t slaph_plan_output_doubles(const slaph_plan *plan, int32_t Lt);
  * dense groups, [8] correlator terms, [9] factor products, [10..12] Q0, Q1, Q2
  * factors, [13] correlator requests, [14] (check_layout != 0) 1 if every
  * trace-value index is written exactly once and every list reads the values
- * of a list with its operands, else 0.  Writes min(n, 15) values. */
+ * of a list with its operands, else 0, [15] tiles of the tensor-core product
+ * plan, [16] (check_layout != 0) 1 if that plan computes every product of
+ * every dependency level exactly once, into its slot, from its left and right
+ * matrices, else 0.  Writes min(n, 17) values. */
 int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
                               int32_t single_block_pair, int32_t check_layout, double *out,
                               int32_t n);

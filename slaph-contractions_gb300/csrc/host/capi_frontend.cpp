@@ -1,4 +1,5 @@
 // C ABI of the host-only parts: errors, front end, readers, HDF5 writer.
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -212,7 +213,7 @@ int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
   return slaph::guarded([&] {
     if (!dims || !plan || !out || n < 0) throw slaph::ArgError("null argument");
     slaph::Schedule const s = slaph::build_schedule(*dims, *plan, single_block_pair);
-    double v[16] = {};
+    double v[17] = {};
     v[0] = static_cast<double>(s.waves.size());
     int64_t lists = 0, uniq = 0, resid = 0, groups = 0;
     for (auto const &w : s.waves) {
@@ -266,7 +267,39 @@ int slaph_plan_schedule_stats(const slaph_dims *dims, const slaph_plan *plan,
       }
       v[14] = ok ? 1.0 : 0.0;
     }
-    for (int32_t i = 0; i < n && i < 16; ++i) out[i] = v[i];
+    // The tensor-core product plan: its tiles, and (check_layout) whether it
+    // computes every product of every level exactly once, into its slot,
+    // from its left and right matrices.
+    int64_t p_tiles = 0;
+    bool p_ok = true;
+    for (auto const &w : s.waves)
+      for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
+        int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
+        slaph::ProductPlan const pp = slaph::plan_products(w.prods.data() + b, e - b, s.eds);
+        p_tiles += pp.n_tiles;
+        if (!check_layout) continue;
+        std::vector<std::tuple<int32_t, int32_t, int32_t>> want, got;
+        for (int64_t k = b; k < e; ++k) want.emplace_back(w.prods[k].a, w.prods[k].b, w.prods[k].c);
+        for (auto const &g : pp.groups) {
+          if (g.n_l < 1 || g.n_l > std::max(1, 64 / s.eds)) p_ok = false;
+          for (int32_t u = 0; u < g.n_u; ++u) {
+            int32_t const r = pp.r_slots[pp.u_list[g.u_off + u]];
+            if (u > 0 && pp.u_list[g.u_off + u] <= pp.u_list[g.u_off + u - 1]) p_ok = false;
+            for (int32_t l = 0; l < 4; ++l) {
+              int32_t const slot = pp.out_tab[4 * (g.u_off + u) + l];
+              if (slot < 0) continue;
+              if (l >= g.n_l) p_ok = false;
+              else got.emplace_back(g.l[l], r, slot);
+            }
+          }
+        }
+        std::sort(want.begin(), want.end());
+        std::sort(got.begin(), got.end());
+        if (want != got) p_ok = false;
+      }
+    v[15] = static_cast<double>(p_tiles);
+    if (check_layout) v[16] = p_ok ? 1.0 : 0.0;
+    for (int32_t i = 0; i < n && i < 17; ++i) out[i] = v[i];
   });
 }
 

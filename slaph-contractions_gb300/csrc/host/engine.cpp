@@ -837,16 +837,12 @@ void Engine::prepare_trace_tc(DeviceSchedule &ds) {
 }
 
 // Tensor-core plan of the factor products (product_tc.cu), per wave and
-// dependency level.  Left matrices are taken in order of first appearance; a
-// group starts with the next unused one and adds, up to 64 / eds, the unused
-// left matrix that shares the most right matrices with the group so far
-// (fewest products computed and dropped).  The group's columns are the union
-// of its members' right matrices in index order.
+// dependency level: the groups of plan_products, their tiles of 80 columns
+// and the scratch they need.
 void Engine::prepare_product_tc(DeviceSchedule &ds) {
   if (ds.p_ready) return;
   Schedule const &s = ds.s;
   int32_t const eds = s.eds;
-  int32_t const per_group = 64 / eds;
   int64_t const a_bytes = dev::prod_tc_a_bytes(eds), r_bytes = dev::prod_tc_r_bytes(eds);
   size_t need = 0;
   int64_t max_expo = 0;
@@ -862,75 +858,20 @@ void Engine::prepare_product_tc(DeviceSchedule &ds) {
       DeviceSchedule::PLevel pl{static_cast<int64_t>(groups.size()), 0,
                                 static_cast<int64_t>(r_slots.size()), 0,
                                 static_cast<int64_t>(tiles.size()), 0};
-      // left matrices (by first appearance) with their (right index, slot)
-      // lists; right matrices numbered by first appearance
-      std::map<int32_t, int32_t> lidx, ridx;
-      std::vector<int32_t> l_slot;
-      std::vector<std::vector<std::pair<int32_t, int32_t>>> lr;
-      int64_t const r0 = static_cast<int64_t>(r_slots.size());
-      for (int64_t k = b; k < e; ++k) {
-        ProdInst const &pi = w.prods[k];
-        auto li = lidx.emplace(pi.a, static_cast<int32_t>(l_slot.size()));
-        if (li.second) {
-          l_slot.push_back(pi.a);
-          lr.emplace_back();
-        }
-        auto ri = ridx.emplace(pi.b, static_cast<int32_t>(r_slots.size() - r0));
-        if (ri.second) r_slots.push_back(pi.b);
-        lr[li.first->second].push_back({ri.first->second, pi.c});
-      }
-      int32_t const n_l = static_cast<int32_t>(l_slot.size());
-      int32_t const n_r = static_cast<int32_t>(r_slots.size() - r0);
-      std::vector<std::vector<int32_t>> inv(n_r);
-      for (int32_t li = 0; li < n_l; ++li) {
-        std::sort(lr[li].begin(), lr[li].end());
-        for (auto const &rc : lr[li]) inv[rc.first].push_back(li);
-      }
-      std::vector<char> used(n_l, 0);
-      std::vector<int32_t> cnt(n_l, 0), touched;
-      for (int32_t li = 0; li < n_l; ++li) {
-        if (used[li]) continue;
-        std::vector<int32_t> mem{li};
-        used[li] = 1;
-        while (static_cast<int32_t>(mem.size()) < per_group) {
-          touched.clear();
-          for (int32_t m : mem)
-            for (auto const &rc : lr[m])
-              for (int32_t l2 : inv[rc.first])
-                if (!used[l2] && cnt[l2]++ == 0) touched.push_back(l2);
-          int32_t best = -1;
-          for (int32_t l2 : touched)
-            if (best < 0 || cnt[l2] > cnt[best] || (cnt[l2] == cnt[best] && l2 < best)) best = l2;
-          for (int32_t l2 : touched) cnt[l2] = 0;
-          if (best < 0) break;
-          mem.push_back(best);
-          used[best] = 1;
-        }
-        std::vector<int32_t> uni;
-        for (int32_t m : mem)
-          for (auto const &rc : lr[m]) uni.push_back(rc.first);
-        std::sort(uni.begin(), uni.end());
-        uni.erase(std::unique(uni.begin(), uni.end()), uni.end());
+      ProductPlan const pp = plan_products(w.prods.data() + b, e - b, eds);
+      int32_t const n_r = static_cast<int32_t>(pp.r_slots.size());
+      r_slots.insert(r_slots.end(), pp.r_slots.begin(), pp.r_slots.end());
+      int32_t const u_base = static_cast<int32_t>(u_list.size());
+      u_list.insert(u_list.end(), pp.u_list.begin(), pp.u_list.end());
+      out_tab.insert(out_tab.end(), pp.out_tab.begin(), pp.out_tab.end());
+      for (auto const &pg : pp.groups) {
         dev::ProdGroup g{};
-        for (int x = 0; x < 4; ++x) g.l[x] = -1;
-        g.n_l = static_cast<int32_t>(mem.size());
-        for (int32_t x = 0; x < g.n_l; ++x) g.l[x] = l_slot[mem[x]];
-        g.n_u = static_cast<int32_t>(uni.size());
-        g.u_off = static_cast<int32_t>(u_list.size());
+        for (int x = 0; x < 4; ++x) g.l[x] = pg.l[x];
+        g.n_l = pg.n_l;
+        g.n_u = pg.n_u;
+        g.u_off = u_base + pg.u_off;
         int32_t const gi = static_cast<int32_t>(groups.size() - pl.g_off);
         g.ea = 64 * gi;
-        for (int32_t u : uni) {
-          u_list.push_back(u);
-          for (int x = 0; x < 4; ++x) {
-            int32_t slot = -1;
-            if (x < g.n_l) {
-              auto const &v = lr[mem[x]];
-              auto it = std::lower_bound(v.begin(), v.end(), std::make_pair(u, INT32_MIN));
-              if (it != v.end() && it->first == u) slot = it->second;
-            }
-            out_tab.push_back(slot);
-          }
-        }
         int32_t const n_t = (eds * g.n_u + dev::kTrTileCols - 1) / dev::kTrTileCols;
         for (int32_t nt = 0; nt < n_t; ++nt) tiles.push_back({gi, nt});
         groups.push_back(g);

@@ -2,6 +2,7 @@
 #include "schedule.hpp"
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <cstdlib>
 #include <exception>
@@ -654,6 +655,82 @@ Schedule build_schedule(slaph_dims const &dims, slaph_plan const &plan, int sing
   if (dims.n_rnd > 16) throw UnsupportedError("at most 16 random vectors (16-bit used masks)");
   Builder b(dims, plan);
   return b.run(single_block_pair);
+}
+
+ProductPlan plan_products(ProdInst const *prods, int64_t n, int32_t eds) {
+  ProductPlan pp;
+  int32_t const per_group = eds > 0 && eds <= 64 ? std::max(1, 64 / eds) : 1;
+  // left matrices (by first appearance) with their (right index, slot)
+  // lists; right matrices numbered by first appearance
+  std::map<int32_t, int32_t> lidx, ridx;
+  std::vector<int32_t> l_slot;
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> lr;
+  for (int64_t k = 0; k < n; ++k) {
+    ProdInst const &pi = prods[k];
+    auto li = lidx.emplace(pi.a, static_cast<int32_t>(l_slot.size()));
+    if (li.second) {
+      l_slot.push_back(pi.a);
+      lr.emplace_back();
+    }
+    auto ri = ridx.emplace(pi.b, static_cast<int32_t>(pp.r_slots.size()));
+    if (ri.second) pp.r_slots.push_back(pi.b);
+    lr[li.first->second].push_back({ri.first->second, pi.c});
+  }
+  int32_t const n_l = static_cast<int32_t>(l_slot.size());
+  std::vector<std::vector<int32_t>> inv(pp.r_slots.size());
+  for (int32_t li = 0; li < n_l; ++li) {
+    std::sort(lr[li].begin(), lr[li].end());
+    for (auto const &rc : lr[li]) inv[rc.first].push_back(li);
+  }
+  std::vector<char> used(n_l, 0);
+  std::vector<int32_t> cnt(n_l, 0), touched;
+  for (int32_t li = 0; li < n_l; ++li) {
+    if (used[li]) continue;
+    std::vector<int32_t> mem{li};
+    used[li] = 1;
+    while (static_cast<int32_t>(mem.size()) < per_group) {
+      touched.clear();
+      for (int32_t m : mem)
+        for (auto const &rc : lr[m])
+          for (int32_t l2 : inv[rc.first])
+            if (!used[l2] && cnt[l2]++ == 0) touched.push_back(l2);
+      int32_t best = -1;
+      for (int32_t l2 : touched)
+        if (best < 0 || cnt[l2] > cnt[best] || (cnt[l2] == cnt[best] && l2 < best)) best = l2;
+      for (int32_t l2 : touched) cnt[l2] = 0;
+      if (best < 0) break;
+      mem.push_back(best);
+      used[best] = 1;
+    }
+    std::vector<int32_t> uni;
+    for (int32_t m : mem)
+      for (auto const &rc : lr[m]) uni.push_back(rc.first);
+    std::sort(uni.begin(), uni.end());
+    uni.erase(std::unique(uni.begin(), uni.end()), uni.end());
+    ProductGroup g{};
+    for (int x = 0; x < 4; ++x) g.l[x] = -1;
+    g.n_l = static_cast<int32_t>(mem.size());
+    for (int32_t x = 0; x < g.n_l; ++x) g.l[x] = l_slot[mem[x]];
+    g.n_u = static_cast<int32_t>(uni.size());
+    if (pp.u_list.size() + uni.size() > 0x7fffffffULL)
+      throw UnsupportedError("product GEMM lists above 2^31");
+    g.u_off = static_cast<int32_t>(pp.u_list.size());
+    for (int32_t u : uni) {
+      pp.u_list.push_back(u);
+      for (int x = 0; x < 4; ++x) {
+        int32_t slot = -1;
+        if (x < g.n_l) {
+          auto const &v = lr[mem[x]];
+          auto it = std::lower_bound(v.begin(), v.end(), std::make_pair(u, INT32_MIN));
+          if (it != v.end() && it->first == u) slot = it->second;
+        }
+        pp.out_tab.push_back(slot);
+      }
+    }
+    pp.n_tiles += (static_cast<int64_t>(eds) * g.n_u + 79) / 80;
+    pp.groups.push_back(g);
+  }
+  return pp;
 }
 
 }  // namespace slaph

@@ -148,6 +148,25 @@ struct Schedule {
 // and 80 B groups); smaller bipartite sets stay residual.
 constexpr int32_t kMinGroupA = 16, kMinGroupB = 16;
 
+// Tensor-core plan of the products of one dependency level (operator*,
+// src/DilutedFactor.cpp:6-51).  Left matrices are taken in order of first
+// appearance; a group starts with the next unused one and adds, up to
+// 64 / eds, the unused left matrix that shares the most right matrices with
+// the group so far.  Column block u of group g is right matrix
+// r_slots[u_list[g.u_off + u]]; out_tab[4 (g.u_off + u) + l] is the slot of
+// product (left matrix l of g) x (that right matrix), or -1 when the level
+// does not ask for it.  n_tiles counts the GEMM tiles of 80 columns.
+struct ProductGroup {
+  int32_t l[4];  // left-matrix slots, n_l of them
+  int32_t n_l, n_u, u_off;
+};
+struct ProductPlan {
+  std::vector<ProductGroup> groups;
+  std::vector<int32_t> r_slots, u_list, out_tab;
+  int64_t n_tiles = 0;
+};
+ProductPlan plan_products(ProdInst const *prods, int64_t n, int32_t eds);
+
 // Builds the schedule; throws EmptyError with the reference's messages when a
 // random-vector combination is empty.  single_block_pair >= 0 restricts the
 // work to that block pair.

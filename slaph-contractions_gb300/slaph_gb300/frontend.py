@@ -154,20 +154,22 @@ class GlobalData:
 
     _STAT_NAMES = ("waves", "trace_lists", "distinct_lists", "residual_lists", "dense_groups",
                    "trace_entries", "distinct_entries", "dense_group_entries", "terms",
-                   "products", "q0", "q1", "q2", "requests", "layout_ok")
+                   "products", "q0", "q1", "q2", "requests", "layout_ok",
+                   "product_tiles", "product_plan_ok")
 
     def schedule_stats(self, single_block_pair=-1, check_layout=False):
         """Counts of the schedule slaph_contract builds for this plan, computed
         on the host (slaph_plan_schedule_stats); with check_layout, also
         whether the trace-value layout is consistent."""
-        out = (C.c_double * 15)()
+        out = (C.c_double * 17)()
         L.check(L.lib().slaph_plan_schedule_stats(C.byref(self.dims), self.plan_ptr,
                                                   single_block_pair, 1 if check_layout else 0,
-                                                  out, 15))
+                                                  out, 17))
         vals = dict(zip(self._STAT_NAMES, out))
         vals = {k: int(v) for k, v in vals.items()}
         if not check_layout:
             vals.pop("layout_ok")
+            vals.pop("product_plan_ok")
         return vals
 
 

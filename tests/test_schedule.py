@@ -9,10 +9,14 @@ def _gd(name):
     return GlobalData.from_infile(w.write_infile())
 
 
-@pytest.mark.parametrize("name", ["cfg1_4x8", "pipi_small", "pipi_groups_e4", "pipi_groups_e8"])
+@pytest.mark.parametrize("name", ["cfg1_4x8", "pipi_small", "pipi_groups_e4", "pipi_groups_e8",
+                                  "pipi_groups_e16"])
 def test_value_layout_is_consistent(engine_lib, name):
     st = _gd(name).schedule_stats(check_layout=True)
     assert st["layout_ok"] == 1
+    # the tensor-core product plan computes each product once, in its slot
+    assert st["product_plan_ok"] == 1
+    assert (st["product_tiles"] > 0) == (st["products"] > 0)
     assert st["distinct_lists"] <= st["trace_lists"]
     assert st["distinct_entries"] <= st["trace_entries"]
     assert st["dense_group_entries"] <= st["distinct_entries"]
