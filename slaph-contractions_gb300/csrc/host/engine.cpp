@@ -1391,6 +1391,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
           sizeof(float4) * ms * std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots);
       df_slots_.reserve(df_bytes);
       df_slots_t_.reserve(df_bytes);
+      slot_expo_.reserve(sizeof(int32_t) *
+                         std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots));
       int64_t const n_vdv = 2LL * static_cast<int64_t>(ops_.size()) * dims_.Lt * nev * nev;
       int64_t const n_noise = 4LL * nev * dims_.Lt * dims_.n_rnd;
       DevBuf vdv_df, noise_df, q0m, q1r;
@@ -1458,6 +1460,10 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
                    "q2_gather");
         count(b.g1[1]); count(b.g2[1]);
       }
+      // exponents of the factor slots for the trace-operand slicing
+      launch(dev::slot_expo(slot_expo_.as<int32_t>(), df_slots_.as<float4>(), 0,
+                            s.n_factor_slots, eds, stream_),
+             "slot_expo");
       SLAPH_CK(cudaEventRecord(ev_[1], stream_));
       SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
     }
@@ -1503,6 +1509,10 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
         } else
           launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
       }
+      if (mixed && w.n_prod_slots > 0)  // exponents of this wave's product slots
+        launch(dev::slot_expo(slot_expo_.as<int32_t>(), df_slots_.as<float4>(),
+                              s.n_factor_slots, w.n_prod_slots, eds, stream_),
+               "slot_expo");
       int64_t const n_res = static_cast<int64_t>(w.residual_lists.size());
       int64_t const n_uni = static_cast<int64_t>(w.unique_lists.size());
       SLAPH_CK(cudaEventRecord(ev_[5], stream_));
@@ -1532,8 +1542,8 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
           cuda_check(dev::trace_tc_slice(tc_scratch_.as<uint8_t>(), tr_expo_.as<int32_t>(),
                                          wb.tc_a.as<dev::TrSliceGroup>() + b.a_off, b.n_a,
                                          wb.tc_b.as<dev::TrSliceGroup>() + b.b_off, b.n_b,
-                                         df_slots_.as<float4>(), df_slots_t_.as<float4>(), eds,
-                                         stream_),
+                                         df_slots_.as<float4>(), df_slots_t_.as<float4>(),
+                                         slot_expo_.as<int32_t>(), eds, stream_),
                      "trace_tc_slice");
           launches_ += (b.n_a > 0 ? 1 : 0) + (b.n_b > 0 ? 1 : 0);
           SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 1], stream_));

@@ -257,13 +257,19 @@ constexpr int32_t kTrTileRows = 64, kTrTileCols = 80;
 int64_t trace_tc_k_tiles(int32_t eds);
 size_t trace_tc_a_bytes(int32_t rows, int32_t eds);  // A region of `rows` matrices
 size_t trace_tc_b_bytes(int32_t cols, int32_t eds);  // B region of `cols` matrices
+// Exponent of each matrix slot first..first+n (double-float, natural
+// layout): expo[slot] = e with |re|, |im| < 2^e over all its entries.  The
+// slicing of the trace operands reads it instead of scanning every matrix
+// again for each group region the matrix appears in.
+cudaError_t slot_expo(int32_t *expo, float4 const *slots, int64_t first, int64_t n, int32_t eds,
+                      cudaStream_t stream);
 // Slices the A matrices (natural layout, conjugated) and B matrices
 // (transposed layout) of a batch into their regions of `scratch`, one row
-// group per CTA.
+// group per CTA, with the exponents of their slots (slot_expo).
 cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSliceGroup const *a_groups,
                            int64_t n_a, TrSliceGroup const *b_groups, int64_t n_b,
-                           float4 const *slots_n, float4 const *slots_t, int32_t eds,
-                           cudaStream_t stream);
+                           float4 const *slots_n, float4 const *slots_t,
+                           int32_t const *slot_expo, int32_t eds, cudaStream_t stream);
 // The GEMM tiles of a batch; FP64 trace values into `values`.
 cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
                           TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,
