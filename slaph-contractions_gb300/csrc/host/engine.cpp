@@ -1391,7 +1391,7 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
           sizeof(float4) * ms * std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots);
       df_slots_.reserve(df_bytes);
       df_slots_t_.reserve(df_bytes);
-      slot_expo_.reserve(sizeof(int32_t) *
+      slot_bits_.reserve(sizeof(unsigned int) *
                          std::max<int64_t>(1, s.n_factor_slots + s.max_prod_slots));
       int64_t const n_vdv = 2LL * static_cast<int64_t>(ops_.size()) * dims_.Lt * nev * nev;
       int64_t const n_noise = 4LL * nev * dims_.Lt * dims_.n_rnd;
@@ -1460,10 +1460,10 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
                    "q2_gather");
         count(b.g1[1]); count(b.g2[1]);
       }
-      // exponents of the factor slots for the trace-operand slicing
-      launch(dev::slot_expo(slot_expo_.as<int32_t>(), df_slots_.as<float4>(), 0,
-                            s.n_factor_slots, eds, stream_),
-             "slot_expo");
+      // largest entries of the factor slots for the trace-operand slicing
+      launch(dev::slot_maxbits(slot_bits_.as<unsigned int>(), df_slots_.as<float4>(), 0,
+                               s.n_factor_slots, eds, stream_),
+             "slot_maxbits");
       SLAPH_CK(cudaEventRecord(ev_[1], stream_));
       SLAPH_CK(cudaEventSynchronize(ev_[1]));  // intermediates are freed here
     }
@@ -1486,6 +1486,11 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
       auto &wb = *ds.waves[wi];
       SLAPH_CK(cudaEventRecord(ev_[2], stream_));
       auto const *prods = wb.prods.as<dev::ProdInst>();
+      // the tensor-core products take the largest entries of their slots by
+      // atomicMax from zero
+      if (p_tc && w.n_prod_slots > 0)
+        SLAPH_CK(cudaMemsetAsync(slot_bits_.as<unsigned int>() + s.n_factor_slots, 0,
+                                 sizeof(unsigned int) * w.n_prod_slots, stream_));
       for (size_t lv = 0; lv + 1 < w.prod_level_off.size(); ++lv) {
         int64_t const b = w.prod_level_off[lv], e = w.prod_level_off[lv + 1];
         if (e <= b) continue;
@@ -1499,7 +1504,7 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
                                   pl.n_g, wb.p_rslots.as<int32_t>() + pl.r_off, pl.n_r,
                                   wb.p_ulist.as<int32_t>(), wb.p_out.as<int32_t>(),
                                   wb.p_tiles.as<dev::ProdTile>() + pl.t_off, pl.n_t, eds,
-                                  err_.as<int>(), stream_),
+                                  slot_bits_.as<unsigned int>(), err_.as<int>(), stream_),
                  "products_tc");
           launches_ += 2;
         } else if (mixed) {
@@ -1509,10 +1514,10 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
         } else
           launch(dev::products(slots_.as<double2>(), prods + b, e - b, eds, stream_), "products");
       }
-      if (mixed && w.n_prod_slots > 0)  // exponents of this wave's product slots
-        launch(dev::slot_expo(slot_expo_.as<int32_t>(), df_slots_.as<float4>(),
-                              s.n_factor_slots, w.n_prod_slots, eds, stream_),
-               "slot_expo");
+      if (mixed && !p_tc && w.n_prod_slots > 0)  // largest entries of the product slots
+        launch(dev::slot_maxbits(slot_bits_.as<unsigned int>(), df_slots_.as<float4>(),
+                                 s.n_factor_slots, w.n_prod_slots, eds, stream_),
+               "slot_maxbits");
       int64_t const n_res = static_cast<int64_t>(w.residual_lists.size());
       int64_t const n_uni = static_cast<int64_t>(w.unique_lists.size());
       SLAPH_CK(cudaEventRecord(ev_[5], stream_));
@@ -1543,7 +1548,7 @@ void Engine::contract(slaph_plan const *plan, int precision, int accumulator,
                                          wb.tc_a.as<dev::TrSliceGroup>() + b.a_off, b.n_a,
                                          wb.tc_b.as<dev::TrSliceGroup>() + b.b_off, b.n_b,
                                          df_slots_.as<float4>(), df_slots_t_.as<float4>(),
-                                         slot_expo_.as<int32_t>(), eds, stream_),
+                                         slot_bits_.as<unsigned int>(), eds, stream_),
                      "trace_tc_slice");
           launches_ += (b.n_a > 0 ? 1 : 0) + (b.n_b > 0 ? 1 : 0);
           SLAPH_CK(cudaEventRecord(tc_ev_[3 * bi + 1], stream_));

@@ -163,7 +163,7 @@ class Engine {
 
   DevBuf V_, peram_, noise_, phase_, phase_fx_, vdv_, ops_dev_, mom_dev_, tc_scratch_, err_;
   HostBuf host_rb_;  // read-back staging
-  DevBuf slot_expo_;  // exponent of every double-float matrix slot (mixed path)
+  DevBuf slot_bits_;  // largest |re|, |im| of every double-float matrix slot (mixed path)
   int read_err_flag();  // the device error flag, through host_rb_ on the engine stream
   std::vector<slaph_vdv_op> ops_;
   DevBuf U_, W_, disp_ops_;  // gauge links, displaced eigenvector scratch, displaced op ids

@@ -194,7 +194,9 @@ cudaError_t products_df(float4 *slots_n, float4 *slots_t, ProdInst const *p, int
 // l x u, or -1 when the level does not ask for it.  Tiles: (group, n tile of
 // 80 columns).  Scratch: the groups' A regions (prod_tc_a_bytes each) from 0,
 // the right-matrix streams (prod_tc_r_bytes each) from r_off; exponents: 64
-// per group from 0, eds per right matrix from r_expo.
+// per group from 0, eds per right matrix from r_expo.  slot_bits (as
+// slot_maxbits; zero for the level's product slots before the call) receives
+// the largest |re|, |im| of every product written.
 struct ProdGroup {
   int32_t l[4];   // left-matrix slots
   int32_t n_l;    // left matrices in the group (1 .. 64 / eds)
@@ -214,7 +216,7 @@ cudaError_t products_tc(float4 *slots_n, float4 *slots_t, uint8_t *scratch, int6
                         int32_t *expo, int64_t r_expo, ProdGroup const *groups, int64_t n_groups,
                         int32_t const *r_slots, int64_t n_r, int32_t const *u_list,
                         int32_t const *out_tab, ProdTile const *tiles, int64_t n_tiles,
-                        int32_t eds, int *err, cudaStream_t stream);
+                        int32_t eds, unsigned int *slot_bits, int *err, cudaStream_t stream);
 // Trace values as double-float pairs (re_hi, re_lo, im_hi, im_lo) into
 // values_df, laid out as for traces().
 cudaError_t traces_df(float4 *values_df, TraceList const *lists, int32_t const *which,
@@ -257,19 +259,19 @@ constexpr int32_t kTrTileRows = 64, kTrTileCols = 80;
 int64_t trace_tc_k_tiles(int32_t eds);
 size_t trace_tc_a_bytes(int32_t rows, int32_t eds);  // A region of `rows` matrices
 size_t trace_tc_b_bytes(int32_t cols, int32_t eds);  // B region of `cols` matrices
-// Exponent of each matrix slot first..first+n (double-float, natural
-// layout): expo[slot] = e with |re|, |im| < 2^e over all its entries.  The
-// slicing of the trace operands reads it instead of scanning every matrix
-// again for each group region the matrix appears in.
-cudaError_t slot_expo(int32_t *expo, float4 const *slots, int64_t first, int64_t n, int32_t eds,
-                      cudaStream_t stream);
+// Largest |re|, |im| of each matrix slot first..first+n (double-float,
+// natural layout, high words) as float bits: the slicing of the trace
+// operands takes each matrix's exponent from it instead of scanning the
+// matrix again for each group region it appears in.
+cudaError_t slot_maxbits(unsigned int *bits, float4 const *slots, int64_t first, int64_t n,
+                         int32_t eds, cudaStream_t stream);
 // Slices the A matrices (natural layout, conjugated) and B matrices
 // (transposed layout) of a batch into their regions of `scratch`, one row
-// group per CTA, with the exponents of their slots (slot_expo).
+// group per CTA, with the largest entries of their slots (slot_maxbits).
 cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSliceGroup const *a_groups,
                            int64_t n_a, TrSliceGroup const *b_groups, int64_t n_b,
                            float4 const *slots_n, float4 const *slots_t,
-                           int32_t const *slot_expo, int32_t eds, cudaStream_t stream);
+                           unsigned int const *slot_bits, int32_t eds, cudaStream_t stream);
 // The GEMM tiles of a batch; FP64 trace values into `values`.
 cudaError_t trace_tc_gemm(double2 *values, uint8_t const *scratch, int32_t const *expo,
                           TrTile const *tiles, int64_t n_tiles, int32_t eds, int *err,

@@ -10,7 +10,8 @@
 //   D(group row (l, i), column (u, j)) = sum_k L_l(i, k) R_u(k, j)
 // gives every product of the group; the epilogue keeps the entries of the
 // pairs the level asks for and writes them as double-float matrices into the
-// product slots, in the natural and the transposed layout.
+// product slots, in the natural and the transposed layout, together with the
+// largest entry of every slot (for the slicing of the trace operands).
 //
 // Operands, in the split-BF16 scheme of tc_common.cuh: A rows are the rows of
 // the left matrices (conjugated, so that the conjugating form gives the plain
@@ -235,6 +236,7 @@ struct ProdEpilogue {
   int64_t r_expo;
   int32_t const *out_tab;  // [group column block][4]: product slot per left matrix
   float4 *slots_n, *slots_t;
+  unsigned int *slot_bits;  // largest |re|, |im| per slot (float bits), by atomicMax
   struct Pre {
     int ok, er, cbase;
     int slot0, ec0, slot1, ec1;
@@ -267,6 +269,15 @@ struct ProdEpilogue {
     int const eds = tl.eds;
     int64_t const ms = static_cast<int64_t>(eds) * eds;
     int const i = (row / 2) % eds;
+    // The slot of a column is the same for the whole warp (one left matrix):
+    // the largest |hi| of a run of columns of one slot goes to slot_bits by
+    // one warp reduction and one atomic.
+    int run_slot = -1;
+    unsigned int run_max = 0;
+    auto flush = [&] {
+      unsigned int const m = __reduce_max_sync(0xffffffffu, run_max);
+      if (run_slot >= 0 && (threadIdx.x % 32) == 0) atomicMax(slot_bits + run_slot, m);
+    };
 #pragma unroll
     for (int cc = 0; cc < kColsW; ++cc) {
       int const slot = __shfl_sync(0xffffffffu, cc < 32 ? p.slot0 : p.slot1, cc % 32);
@@ -275,21 +286,29 @@ struct ProdEpilogue {
       float const h = scale2(hi[cc], sh), lw = scale2(lo[cc], sh);
       float const oh = __shfl_xor_sync(0xffffffffu, h, 1);
       float const ol = __shfl_xor_sync(0xffffffffu, lw, 1);
+      if (slot != run_slot) {  // warp-uniform
+        flush();
+        run_slot = slot;
+        run_max = 0;
+      }
       if (slot < 0) continue;
+      run_max = max(run_max, __float_as_uint(h) & 0x7FFFFFFFu);
       int const j = (p.cbase + cc) % eds;
       if ((row & 1) == 0)
         slots_n[slot * ms + i + static_cast<int64_t>(eds) * j] = make_float4(h, lw, oh, ol);
       else
         slots_t[slot * ms + j + static_cast<int64_t>(eds) * i] = make_float4(oh, ol, h, lw);
     }
+    flush();
   }
 };
 
 __global__ void __launch_bounds__(kThreads, 1)
     product_gemm_kernel(ProdTiles tl, int32_t n_tiles, int32_t const *expo, int64_t r_expo,
-                        int32_t const *out_tab, float4 *slots_n, float4 *slots_t, int *err) {
+                        int32_t const *out_tab, float4 *slots_n, float4 *slots_t,
+                        unsigned int *slot_bits, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  ProdEpilogue epi{tl, expo, r_expo, out_tab, slots_n, slots_t};
+  ProdEpilogue epi{tl, expo, r_expo, out_tab, slots_n, slots_t, slot_bits};
   ozaki_tiles(smem, n_tiles, tl.k_tiles, tl, err, epi);
 }
 
@@ -304,7 +323,7 @@ cudaError_t products_tc(float4 *slots_n, float4 *slots_t, uint8_t *scratch, int6
                         int32_t *expo, int64_t r_expo, ProdGroup const *groups, int64_t n_groups,
                         int32_t const *r_slots, int64_t n_r, int32_t const *u_list,
                         int32_t const *out_tab, ProdTile const *tiles, int64_t n_tiles,
-                        int32_t eds, int *err, cudaStream_t stream) {
+                        int32_t eds, unsigned int *slot_bits, int *err, cudaStream_t stream) {
   if (n_tiles == 0) return cudaSuccess;
   if (!prod_tc_supported(eds) || n_groups > 0x7fffffffLL || n_r > 0x7fffffffLL ||
       n_tiles > 0x7fffffffLL)
@@ -322,7 +341,7 @@ cudaError_t products_tc(float4 *slots_n, float4 *slots_t, uint8_t *scratch, int6
   ProdTiles const tl{scratch, a_bytes, r_off, tiles, groups, u_list, eds, eds / (kTK / 2)};
   product_gemm_kernel<<<static_cast<unsigned>(persistent_grid(n_tiles)), kThreads, kSmemBytes,
                         stream>>>(tl, static_cast<int32_t>(n_tiles), expo, r_expo, out_tab,
-                                  slots_n, slots_t, err);
+                                  slots_n, slots_t, slot_bits, err);
   return cudaGetLastError();
 }
 

@@ -32,12 +32,12 @@ using namespace tc;
 
 constexpr int kSliceThreads = 256;  // eight warps per row group
 
-// Exponent of every matrix slot first..first+n: e with |re|, |im| < 2^e for
-// all its entries (from the high words; |hi + lo| < 2^e whenever |hi| < 2^e,
-// as |lo| <= ulp(hi) / 2).  One warp per slot.
+// Largest |re|, |im| of every matrix slot first..first+n, as the bit pattern
+// of the float (from the high words; |hi + lo| < 2^e whenever |hi| < 2^e, as
+// |lo| <= ulp(hi) / 2).  One warp per slot.
 __global__ void __launch_bounds__(256)
-    slot_expo_kernel(int32_t *expo, float4 const *slots, int64_t first, int64_t n,
-                     int32_t eds) {
+    slot_maxbits_kernel(unsigned int *bits, float4 const *slots, int64_t first, int64_t n,
+                        int32_t eds) {
   int64_t const w = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / 32;
   int const lane = threadIdx.x % 32;
   if (w >= n) return;
@@ -50,11 +50,11 @@ __global__ void __launch_bounds__(256)
     mx = max(mx, max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.z) & 0x7FFFFFFFu));
   }
   mx = __reduce_max_sync(0xffffffffu, mx);
-  if (lane == 0) expo[first + w] = expo_of_absbits(mx);
+  if (lane == 0) bits[first + w] = mx;
 }
 
 // One row group per CTA (TrSliceGroup), one pass over its matrices with the
-// exponents of their slots (slot_expo_kernel): the warps take k-tiles in
+// largest entries of their slots (slot_maxbits): the warps take k-tiles in
 // turn.  In a k-tile, lane (r, kc) = (lane / 4, lane % 4) converts the four
 // complex entries 4 kc .. 4 kc + 3 of core-matrix row r (B: matrix r; A:
 // matrix r / 2, A' row parity r % 2) into one 16-byte row segment per slice,
@@ -65,18 +65,19 @@ __global__ void __launch_bounds__(256)
 template <bool kIsA>
 __global__ void __launch_bounds__(kSliceThreads)
     trace_slice_kernel(uint8_t *scratch, int32_t *expo, TrSliceGroup const *groups,
-                       float4 const *slots, int32_t const *slot_expo, int32_t eds) {
+                       float4 const *slots, unsigned int const *slot_bits, int32_t eds) {
   TrSliceGroup const gr = groups[blockIdx.x];
   int64_t const ms = static_cast<int64_t>(eds) * eds;
   int32_t const k_tiles = static_cast<int32_t>(ms / (kTK / 2));
   int const warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (threadIdx.x < gr.n)
-    expo[gr.expo0 + threadIdx.x] = slot_expo[groups[blockIdx.x].slot[threadIdx.x]];
+    expo[gr.expo0 + threadIdx.x] =
+        expo_of_absbits(slot_bits[groups[blockIdx.x].slot[threadIdx.x]]);
   int const r = lane / 4, kc = lane % 4;
   int const mi = kIsA ? r / 2 : r;  // matrix of this lane
   if (mi >= gr.n) return;
   int const slot = groups[blockIdx.x].slot[mi];
-  int const e = slot_expo[slot];
+  int const e = expo_of_absbits(slot_bits[slot]);
   float4 const *src = slots + static_cast<int64_t>(slot) * ms + 4 * kc;
   uint8_t *region = scratch + gr.dst;
   uint8_t *base;
@@ -194,25 +195,25 @@ size_t trace_tc_b_bytes(int32_t cols, int32_t eds) {
   return static_cast<size_t>((cols + kTN - 1) / kTN) * trace_tc_k_tiles(eds) * kStageB;
 }
 
-cudaError_t slot_expo(int32_t *expo, float4 const *slots, int64_t first, int64_t n, int32_t eds,
-                      cudaStream_t stream) {
+cudaError_t slot_maxbits(unsigned int *bits, float4 const *slots, int64_t first, int64_t n,
+                         int32_t eds, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  slot_expo_kernel<<<static_cast<unsigned>((n * 32 + 255) / 256), 256, 0, stream>>>(
-      expo, slots, first, n, eds);
+  slot_maxbits_kernel<<<static_cast<unsigned>((n * 32 + 255) / 256), 256, 0, stream>>>(
+      bits, slots, first, n, eds);
   return cudaGetLastError();
 }
 
 cudaError_t trace_tc_slice(uint8_t *scratch, int32_t *expo, TrSliceGroup const *a_groups,
                            int64_t n_a, TrSliceGroup const *b_groups, int64_t n_b,
                            float4 const *slots_n, float4 const *slots_t,
-                           int32_t const *slot_expo, int32_t eds, cudaStream_t stream) {
+                           unsigned int const *slot_bits, int32_t eds, cudaStream_t stream) {
   if ((static_cast<int64_t>(eds) * eds) % (kTK / 2) != 0) return cudaErrorInvalidValue;
   if (n_a > 0)
     trace_slice_kernel<true><<<static_cast<unsigned>(n_a), kSliceThreads, 0, stream>>>(
-        scratch, expo, a_groups, slots_n, slot_expo, eds);
+        scratch, expo, a_groups, slots_n, slot_bits, eds);
   if (n_b > 0)
     trace_slice_kernel<false><<<static_cast<unsigned>(n_b), kSliceThreads, 0, stream>>>(
-        scratch, expo, b_groups, slots_t, slot_expo, eds);
+        scratch, expo, b_groups, slots_t, slot_bits, eds);
   return cudaGetLastError();
 }
 
