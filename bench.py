@@ -60,6 +60,32 @@ def per_correlator_rel_err(out, ref):
     return float(np.max(rel)) if rel.size else 0.0
 
 
+# Host bytes up to which the VdaggerV blocks of a build are kept for the
+# comparison of the two paths (32^3x64: 33 operators x 64 timeslices x
+# 220^2 x 16 B = 1.6 GB).
+VDV_CHECK_MAX_BYTES = 8e9
+
+
+def vdaggerv_snapshot(eng, n_ops, Lt):
+    """Every VdaggerV block (operator, timeslice) of the engine's last build."""
+    return [eng.vdaggerv_fetch(op, t) for op in range(n_ops) for t in range(Lt)]
+
+
+def vdaggerv_max_rel_err(eng, n_ops, Lt, snapshot):
+    """Largest error of the snapshot's blocks against the engine's current
+    build, each block by the largest |entry| of the current one (its
+    absolute error for a zero block)."""
+    err, k = 0.0, 0
+    for op in range(n_ops):
+        for t in range(Lt):
+            ref = eng.vdaggerv_fetch(op, t)
+            d = float(np.max(np.abs(snapshot[k] - ref)))
+            m = float(np.max(np.abs(ref)))
+            err = max(err, d / m if m > 0 else d)
+            k += 1
+    return err
+
+
 def workload_config(w, n_correlators, single_block_pair, world):
     """The workload's description, printed identically by both arms."""
     return {"workload": w.name, "lattice": f"{w.L}^3x{w.Lt}", "nev": w.nev,
@@ -355,12 +381,30 @@ def run_engine(args):
     # result against it, relative per correlator.
     fp64 = None
     if precision == 1 and not args.no_fp64_check:
+        # The VdaggerV blocks of the last split-precision build (the
+        # contraction leaves them in place), against the FP64 build of the
+        # same eigenvectors below: every operator and timeslice.
+        n_vdv_ops = int(gd.plan.n_vdv_ops)
+        vdv_snap, vdv_err, vdv_note = None, None, None
+        if n_vdv_ops * w.Lt * 16 * w.nev ** 2 <= VDV_CHECK_MAX_BYTES:
+            try:
+                vdv_snap = vdaggerv_snapshot(eng, n_vdv_ops, w.Lt)
+            except Exception as exc:  # reported in the line, never fatal
+                vdv_note = f"not compared: {exc}"
+        else:
+            vdv_note = f"not compared: blocks above {VDV_CHECK_MAX_BYTES:.0e} host bytes"
         w0 = time.time()
         eng.vdaggerv_build(0)
         t_v = eng.timings()
         out64 = eng.contract(gd.plan_ptr, 0, 0, args.single_block_pair)
         t_c = eng.timings()
         wall64 = time.time() - w0
+        if vdv_snap is not None:
+            try:
+                vdv_err = vdaggerv_max_rel_err(eng, n_vdv_ops, w.Lt, vdv_snap)
+            except Exception as exc:
+                vdv_note = f"not compared: {exc}"
+            vdv_snap = None
         # the same (FP64) HYP smearing precedes both builds
         st64 = [t_v[0], t_c[1], t_c[2], t_c[3], stage[4] / args.steps]
         fp64 = {"value": float(sum(st64)) / 1e3, "unit": UNIT,
@@ -370,7 +414,12 @@ def run_engine(args):
                 "max_rel_err_vs_fp64": per_correlator_rel_err(out, out64),
                 "n_correlators": int(out64.shape[0]),
                 "error_measure": ("max over correlators of max_t |mixed - fp64| / "
-                                  "max_t |fp64| (each HDF5 dataset by its own scale)")}
+                                  "max_t |fp64| (each HDF5 dataset by its own scale)"),
+                "vdaggerv_max_rel_err_vs_fp64": vdv_err,
+                "vdaggerv_blocks": n_vdv_ops * w.Lt if vdv_err is not None else 0,
+                "vdaggerv_error_measure": (vdv_note or
+                                           "max over (operator, timeslice) blocks of "
+                                           "max |mixed - fp64| / max |fp64 block|")}
 
     stats = eng.stats()
     n_ops = gd.plan.n_vdv_ops - (1 if gd.plan.index_of_unity >= 0 else 0)
