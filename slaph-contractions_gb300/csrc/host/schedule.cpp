@@ -10,7 +10,7 @@
 #include <mutex>
 #include <thread>
 #include <tuple>
-#include <unordered_map>
+#include <unordered_set>
 
 #include "capi_util.hpp"
 
@@ -56,6 +56,67 @@ inline uint64_t pack2(int64_t a, int64_t b) {
   return (static_cast<uint64_t>(static_cast<uint32_t>(a)) << 32) | static_cast<uint32_t>(b);
 }
 
+// Memo from 64-bit keys: open addressing with linear probing in a
+// power-of-two table at most half full (the symbolic replay looks keys up
+// some 10^8 times per plan; a node-based map spends most of that time in cache
+// misses).
+template <typename V>
+class Memo64 {
+ public:
+  V const *find(uint64_t key) const {
+    if (n_ == 0) return nullptr;
+    for (size_t i = slot_of(key);; i = (i + 1) & mask_) {
+      Slot const &s = slots_[i];
+      if (!s.used) return nullptr;
+      if (s.key == key) return &s.val;
+    }
+  }
+  // Inserts a key that is not present.
+  void emplace(uint64_t key, V const &val) {
+    if (2 * (n_ + 1) > slots_.size()) grow();
+    insert(key, val);
+  }
+  void clear() {
+    if (n_ == 0) return;
+    for (auto &s : slots_) s.used = false;
+    n_ = 0;
+  }
+
+ private:
+  struct Slot {
+    uint64_t key;
+    V val;
+    bool used;
+  };
+  std::vector<Slot> slots_;
+  size_t n_ = 0, mask_ = 0;
+
+  size_t slot_of(uint64_t k) const {
+    // 64-bit mixing (the finaliser of MurmurHash3)
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdULL;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ULL;
+    k ^= k >> 33;
+    return static_cast<size_t>(k) & mask_;
+  }
+  void insert(uint64_t key, V const &val) {
+    size_t i = slot_of(key);
+    while (slots_[i].used) i = (i + 1) & mask_;
+    slots_[i] = Slot{key, val, true};
+    ++n_;
+  }
+  void grow() {
+    std::vector<Slot> old;
+    old.swap(slots_);
+    slots_.assign(old.empty() ? 1024 : 2 * old.size(), Slot{0, V{}, false});
+    mask_ = slots_.size() - 1;
+    n_ = 0;
+    for (auto const &s : old)
+      if (s.used) insert(s.key, s.val);
+  }
+};
+
 class Builder {
  public:
   Builder(slaph_dims const &d, slaph_plan const &p) : dims_(d), plan_(p) {
@@ -76,22 +137,52 @@ class Builder {
       total += plan_.diagrams[d].n_requests;
     }
     s_.n_outputs = total;
+    // Per diagram, its requests' trace references numbered by (kind, trace
+    // id, locations): equal references give the same trace list within a
+    // slice pair, so each is resolved once per slice pair, at its first use
+    // in request order (the order in which lists are created is unchanged).
+    std::vector<std::vector<int32_t>> ref_of(plan_.n_diagrams);
+    std::vector<int32_t> n_refs(plan_.n_diagrams, 0);
+    for (int d = 0; d < plan_.n_diagrams; ++d) {
+      auto const &dg = plan_.diagrams[d];
+      std::map<std::array<int32_t, 9>, int32_t> ids;
+      for (int i = 0; i < dg.n_requests; ++i) {
+        auto const &req = dg.requests[i];
+        if (req.n_traces < 1 || req.n_traces > 3) continue;  // rejected below
+        for (int k = 0; k < req.n_traces; ++k) {
+          auto const &r = req.traces[k];
+          std::array<int32_t, 9> key{r.kind, r.tr_id, r.n_loc, 0, 0, 0, 0, 0, 0};
+          for (int l = 0; l < std::min(std::max(r.n_loc, 0), 6); ++l) key[3 + l] = r.loc[l];
+          ref_of[d].push_back(ids.emplace(key, static_cast<int32_t>(ids.size())).first->second);
+        }
+      }
+      n_refs[d] = static_cast<int32_t>(ids.size());
+    }
     for (int b = 0; b < n_bp; ++b) {
       if (single_block_pair >= 0 && b != single_block_pair) continue;
       begin_wave(b);
       auto const slices = slice_pairs(b, nb);
+      w_.terms.reserve(static_cast<size_t>(total) * slices.size());
+      tlist_memo_.resize(slices.size());
       for (int d = 0; d < plan_.n_diagrams; ++d) {
         auto const &dg = plan_.diagrams[d];
-        for (auto const &sp : slices) {
+        std::vector<int32_t> ref_list(n_refs[d]);
+        for (size_t spi = 0; spi < slices.size(); ++spi) {
+          auto const &sp = slices[spi];
           int const dt = std::abs((sp.second - sp.first - Lt) % Lt);
+          std::fill(ref_list.begin(), ref_list.end(), -1);
+          size_t pos = 0;
           for (int i = 0; i < dg.n_requests; ++i) {
             auto const &req = dg.requests[i];
             if (req.n_traces < 1 || req.n_traces > 3)
               throw UnsupportedError("This many traces are not implemented yet.");
             Term t{};
             t.n = req.n_traces;
-            for (int k = 0; k < req.n_traces; ++k)
-              t.list[k] = trace_list(req.traces[k], sp.first, sp.second);
+            for (int k = 0; k < req.n_traces; ++k) {
+              int32_t &id = ref_list[ref_of[d][pos++]];
+              if (id < 0) id = trace_list(req.traces[k], sp.first, sp.second, tlist_memo_[spi]);
+              t.list[k] = id;
+            }
             if (req.n_traces > 1) check_inner_product(t);
             t.out = static_cast<int32_t>(offset[d] + i);
             t.dt = dt;
@@ -114,16 +205,18 @@ class Builder {
 
   std::vector<std::vector<SymE>> shapes_;
   std::map<std::vector<SymE>, int32_t> shape_ids_;
-  std::unordered_map<uint64_t, int32_t> fshape_memo_;     // (type, ql) -> shape
-  std::unordered_map<uint64_t, int32_t> ptemplate_memo_;  // (shapeL, shapeR) -> template
+  Memo64<int32_t> fshape_memo_;     // (type, ql) -> shape
+  Memo64<int32_t> ptemplate_memo_;  // (shapeL, shapeR) -> template
   std::vector<ProdTemplate> ptemplates_;
-  std::unordered_map<uint64_t, int32_t> tshape_memo_;     // (shapeL, shapeR|-1) -> trace shape
+  Memo64<int32_t> tshape_memo_;     // (shapeL, shapeR|-1) -> trace shape
   std::vector<int32_t> tshape_ip_checked_;
-  std::map<std::vector<int32_t>, bool> ip_checked_;
+  std::unordered_set<uint64_t> ip_checked_;  // shape tuples already checked
 
-  std::unordered_map<uint64_t, ListRef> flist_memo_;  // factor lists, global
-  std::unordered_map<uint64_t, ListRef> plist_memo_;  // product lists, per wave
-  std::unordered_map<uint64_t, int32_t> tlist_memo_;  // trace lists, per wave
+  Memo64<ListRef> flist_memo_;  // factor lists, global
+  Memo64<ListRef> plist_memo_;  // product lists, per wave
+  // trace lists of the wave, one memo per slice pair (a slice pair's lookups
+  // stay within its own small table)
+  std::vector<Memo64<int32_t>> tlist_memo_;
   std::vector<int32_t> list_shape_;                   // trace list -> trace shape (wave)
   std::map<std::tuple<int, int, int>, int32_t> q0m_memo_, q1r_memo_;
   std::map<std::tuple<int, int, int, int>, int32_t> q2m_memo_;
@@ -161,7 +254,7 @@ class Builder {
     wave_prod_slots_ = 0;
     wave_prods_.clear();
     plist_memo_.clear();
-    tlist_memo_.clear();
+    tlist_memo_.clear();  // sized per wave by run()
     list_shape_.clear();
   }
 
@@ -261,16 +354,28 @@ class Builder {
   // then the residual lists one after another.
   void group_lists(Wave &w) {
     int64_t const n = static_cast<int64_t>(w.lists.size());
+    // Lists in order of (shape, a_base, b_base, index), sorted as compact
+    // records (the keys next to the index, not behind it).
+    struct ListKey {
+      int32_t shape, a, b, k;
+      bool operator<(ListKey const &o) const {
+        return std::tie(shape, a, b, k) < std::tie(o.shape, o.a, o.b, o.k);
+      }
+    };
     std::vector<int32_t> ord(n);
-    for (int64_t k = 0; k < n; ++k) ord[k] = static_cast<int32_t>(k);
+    {
+      std::vector<ListKey> keys(n);
+      for (int64_t k = 0; k < n; ++k) {
+        auto const &l = w.lists[k];
+        keys[k] = {l.shape, l.a_base, l.b_base, static_cast<int32_t>(k)};
+      }
+      std::sort(keys.begin(), keys.end());
+      for (int64_t p = 0; p < n; ++p) ord[p] = keys[p].k;
+    }
     auto key = [&](int32_t k) {
       auto const &l = w.lists[k];
       return std::make_tuple(l.shape, l.a_base, l.b_base);
     };
-    std::sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) {
-      auto const kx = key(x), ky = key(y);
-      return kx != ky ? kx < ky : x < y;
-    });
     // canonical[k]: the lowest-numbered list with the operands of list k.
     std::vector<int32_t> canonical(n);
     std::vector<int32_t> uniq;  // canonical lists in key order
@@ -311,13 +416,24 @@ class Builder {
           return false;
       return true;
     };
+    // Runs in order of (shape, B-set hash, B-set size), ties in run order.
+    struct RunKey {
+      int32_t shape, k;
+      uint64_t hash;
+      int64_t size;
+      bool operator<(RunKey const &o) const {
+        return std::tie(shape, hash, size, k) < std::tie(o.shape, o.hash, o.size, o.k);
+      }
+    };
     std::vector<int32_t> run_ord(runs.size());
-    for (size_t k = 0; k < runs.size(); ++k) run_ord[k] = static_cast<int32_t>(k);
-    std::stable_sort(run_ord.begin(), run_ord.end(), [&](int32_t x, int32_t y) {
-      auto const &a = runs[x], &b = runs[y];
-      return std::make_tuple(a.shape, a.hash, a.end - a.begin) <
-             std::make_tuple(b.shape, b.hash, b.end - b.begin);
-    });
+    {
+      std::vector<RunKey> keys(runs.size());
+      for (size_t k = 0; k < runs.size(); ++k)
+        keys[k] = {runs[k].shape, static_cast<int32_t>(k), runs[k].hash,
+                   runs[k].end - runs[k].begin};
+      std::sort(keys.begin(), keys.end());
+      for (size_t p = 0; p < keys.size(); ++p) run_ord[p] = keys[p].k;
+    }
     std::vector<char> in_group(n, 0);
     w.groups.clear();
     w.group_bases.clear();
@@ -419,8 +535,7 @@ class Builder {
                          (static_cast<uint64_t>(a & 0x3FF) << 52) |
                          (static_cast<uint64_t>(b & 0x3FF) << 42) |
                          (static_cast<uint64_t>(c & 0x3FF) << 32) | static_cast<uint32_t>(ql);
-    auto it = flist_memo_.find(key);
-    if (it != flist_memo_.end()) return it->second;
+    if (ListRef const *hit = flist_memo_.find(key)) return *hit;
     auto const &o = op(type, ql);
     int32_t const vdv = vdv_code(o);
     int32_t const base = n_factor_slots_;
@@ -444,13 +559,12 @@ class Builder {
       entries.push_back({r1, r2, 0});
     }
     uint64_t const skey = pack2(type, ql);
-    auto sit = fshape_memo_.find(skey);
     int32_t shape;
-    if (sit == fshape_memo_.end()) {
+    if (int32_t const *hit = fshape_memo_.find(skey)) {
+      shape = *hit;
+    } else {
       shape = shape_id(entries);
       fshape_memo_.emplace(skey, shape);
-    } else {
-      shape = sit->second;
     }
     ListRef ref{shape, base, 0};
     flist_memo_.emplace(key, ref);
@@ -463,8 +577,7 @@ class Builder {
   // operator*(vector<DF>, vector<DF>), src/DilutedFactor.cpp:6-51.
   ProdTemplate const &product_template(int32_t sl, int32_t sr) {
     uint64_t const key = pack2(sl, sr);
-    auto it = ptemplate_memo_.find(key);
-    if (it != ptemplate_memo_.end()) return ptemplates_[it->second];
+    if (int32_t const *hit = ptemplate_memo_.find(key)) return ptemplates_[*hit];
     ProdTemplate t;
     std::vector<SymE> out;
     auto const &L = shapes_[sl];
@@ -488,8 +601,7 @@ class Builder {
   // multiply<1,1> memo (include/DilutedFactor.hpp:164-187), per wave.
   ListRef multiply(ListRef const &l, ListRef const &r) {
     uint64_t const key = pack2(l.base, r.base);
-    auto it = plist_memo_.find(key);
-    if (it != plist_memo_.end()) return it->second;
+    if (ListRef const *hit = plist_memo_.find(key)) return *hit;
     ProdTemplate const &t = product_template(l.shape, r.shape);
     int32_t const level = std::max(l.level, r.level) + 1;
     int32_t const base = -(wave_prod_slots_ + 1);
@@ -508,8 +620,7 @@ class Builder {
   // factor_to_trace(L, R) / factor_to_trace(F), src/DilutedTrace.cpp:84-165.
   int32_t trace_shape(int32_t sl, int32_t sr) {
     uint64_t const key = pack2(sl, sr);
-    auto it = tshape_memo_.find(key);
-    if (it != tshape_memo_.end()) return it->second;
+    if (int32_t const *hit = tshape_memo_.find(key)) return *hit;
     TraceShape ts;
     auto const &L = shapes_[sl];
     if (sr >= 0) {
@@ -597,7 +708,7 @@ class Builder {
     }
   }
 
-  int32_t trace_list(slaph_trace_request const &r, int src, int snk) {
+  int32_t trace_list(slaph_trace_request const &r, int src, int snk, Memo64<int32_t> &memo) {
     static int const arity[SLAPH_TR_KINDS] = {1, 2, 2, 3, 3, 4, 4, 6};
     if (r.kind < 0 || r.kind >= SLAPH_TR_KINDS) throw ArgError("unknown trace kind");
     if (r.tr_id < 0 || r.tr_id >= plan_.n_trace_ids[r.kind] || r.tr_id >= (1 << 24))
@@ -613,22 +724,26 @@ class Builder {
                          (static_cast<uint64_t>(src & 0x3FF) << 27) |
                          (static_cast<uint64_t>(snk & 0x3FF) << 17) |
                          static_cast<uint64_t>(src == snk ? 0 : pattern);
-    auto it = tlist_memo_.find(key);
-    if (it != tlist_memo_.end()) return it->second;
+    if (int32_t const *hit = memo.find(key)) return *hit;
     int k[6];
     for (int l = 0; l < r.n_loc; ++l) k[l] = r.loc[l] == 0 ? src : snk;
     int const *c = plan_.trace_ql_ids[r.kind] + static_cast<int64_t>(r.tr_id) * arity[r.kind];
     int32_t const id = build_trace(r.kind, k, c);
-    tlist_memo_.emplace(key, id);
+    memo.emplace(key, id);
     return id;
   }
 
   // inner_product must have at least one summand (src/DilutedTrace.cpp:37-41,
   // 75-79).  Masks depend only on the trace shapes, so the check is memoised.
   void check_inner_product(Term const &t) {
-    std::vector<int32_t> key(t.n);
+    int32_t key[3] = {0, 0, 0};
     for (int k = 0; k < t.n; ++k) key[k] = list_shape_[t.list[k]];
-    if (ip_checked_.count(key)) return;
+    if (key[0] >= (1 << 21) || key[1] >= (1 << 21) || key[2] >= (1 << 21))
+      throw UnsupportedError("more than 2^21 trace shapes");
+    uint64_t const packed = (static_cast<uint64_t>(t.n == 3 ? 1 : 0) << 63) |
+                            (static_cast<uint64_t>(key[0]) << 42) |
+                            (static_cast<uint64_t>(key[1]) << 21) | static_cast<uint64_t>(key[2]);
+    if (ip_checked_.count(packed)) return;
     auto const &a = s_.shapes[key[0]].mask;
     auto const &b = s_.shapes[key[1]].mask;
     bool any = false;
@@ -642,7 +757,7 @@ class Builder {
           for (auto z : c) any = any || (x & y & z) == 0;
     }
     if (!any) throw EmptyError(kIpEmpty);
-    ip_checked_.emplace(key, true);
+    ip_checked_.insert(packed);
   }
 };
 
