@@ -28,11 +28,13 @@ struct SymE {
 };
 
 // Concrete list: entry e lives in matrix slot base + e.  Product slots are
-// encoded as -(local + 1) until the factor slot count is final.
+// encoded as -(local + 1) until the factor slot count is final.  t: the
+// timeslice of the list's first factor (of its left operand for a product).
 struct ListRef {
   int32_t shape;
   int32_t base;
   int32_t level;
+  int32_t t;
 };
 
 struct ProdTemplate {
@@ -213,7 +215,9 @@ class Builder {
   std::unordered_set<uint64_t> ip_checked_;  // shape tuples already checked
 
   Memo64<ListRef> flist_memo_;  // factor lists, global
-  Memo64<ListRef> plist_memo_;  // product lists, per wave
+  // product lists of the wave, by the timeslice of the left operand (the key
+  // decides it; a slice pair's lookups stay within two small tables)
+  std::vector<Memo64<ListRef>> plist_memo_;
   // trace lists of the wave, one memo per slice pair (a slice pair's lookups
   // stay within its own small table)
   std::vector<Memo64<int32_t>> tlist_memo_;
@@ -253,7 +257,7 @@ class Builder {
     w_.block_pair = b;
     wave_prod_slots_ = 0;
     wave_prods_.clear();
-    plist_memo_.clear();
+    plist_memo_.assign(static_cast<size_t>(dims_.Lt), Memo64<ListRef>{});
     tlist_memo_.clear();  // sized per wave by run()
     list_shape_.clear();
   }
@@ -566,7 +570,7 @@ class Builder {
       shape = shape_id(entries);
       fshape_memo_.emplace(skey, shape);
     }
-    ListRef ref{shape, base, 0};
+    ListRef ref{shape, base, 0, a};
     flist_memo_.emplace(key, ref);
     return ref;
   }
@@ -601,7 +605,8 @@ class Builder {
   // multiply<1,1> memo (include/DilutedFactor.hpp:164-187), per wave.
   ListRef multiply(ListRef const &l, ListRef const &r) {
     uint64_t const key = pack2(l.base, r.base);
-    if (ListRef const *hit = plist_memo_.find(key)) return *hit;
+    Memo64<ListRef> &memo = plist_memo_[static_cast<size_t>(l.t)];
+    if (ListRef const *hit = memo.find(key)) return *hit;
     ProdTemplate const &t = product_template(l.shape, r.shape);
     int32_t const level = std::max(l.level, r.level) + 1;
     int32_t const base = -(wave_prod_slots_ + 1);
@@ -612,8 +617,8 @@ class Builder {
       int32_t const b = r.base >= 0 ? r.base + pr.second : r.base - pr.second;
       wave_prods_.push_back({level, ProdInst{a, b, slot}});
     }
-    ListRef ref{t.out_shape, base, level};
-    plist_memo_.emplace(key, ref);
+    ListRef ref{t.out_shape, base, level, l.t};
+    memo.emplace(key, ref);
     return ref;
   }
 
